@@ -1,0 +1,135 @@
+/*
+ * tnx -- C ABI of the GB300 (sm_103a) DMRG / tSDRG numerical core.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (as void*), returns a tnx_status code, and never throws. Buffers are owned
+ * by the caller; workspace is passed in explicitly and its size is given by
+ * the matching *_workspace_bytes query. The library allocates no device memory
+ * on any of these paths. tnx_last_error() returns a thread-local message for the
+ * last failing call on the calling thread.
+ *
+ * Tensor layouts (row-major, FP64 unless stated):
+ *   MPS site tensor  A[chi_l][d][chi_r]            ('lpr', tnpy/matrix_product_state.py:45)
+ *   MPO site tensor  W[dl][dr][d][d]  (l, r, ket, bra; boundary tensors carry a 1-sized dl / dr)
+ *   environments     L[chi_l][dl][chi_l], R[chi_r][dr][chi_r]  (ket, mpo, bra; 1x1x1 ones on
+ *                    the open ends)
+ */
+#ifndef TNX_H_
+#define TNX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum tnx_status {
+  TNX_OK = 0,
+  TNX_ERR_INVALID_ARG = 1,   /* null pointer, non-positive size, bad enum   (reference: ValueError) */
+  TNX_ERR_SHAPE = 2,         /* inconsistent or unsupported dimensions      (reference: ValueError) */
+  TNX_ERR_WORKSPACE = 3,     /* workspace smaller than *_workspace_bytes    */
+  TNX_ERR_NOT_CONVERGED = 4, /* iteration limit reached (result still written) */
+  TNX_ERR_CUDA = 5,          /* a CUDA launch or copy failed                */
+  TNX_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up          */
+  TNX_ERR_UNSUPPORTED = 7    /* precision / size not built into this library */
+};
+
+enum tnx_precision {
+  TNX_FP64 = 0,       /* plain FP64 contractions (CUDA cores)                         */
+  TNX_BF16X3 = 1      /* split-BF16 three-term products on tcgen05, FP32 accumulation  */
+};
+
+const char* tnx_status_string(int status);
+const char* tnx_last_error(void);
+int tnx_version(void);
+/* 1 when the loaded library was built for sm_103a and a device of compute capability
+ * 10.3 is current; 0 otherwise. */
+int tnx_device_ok(void);
+
+/* ---- one-site effective Hamiltonian ------------------------------------------------
+ * Replaces Environment.one_site_matvec (tnpy/matrix_product_state.py:411-440):
+ *   y[a',s',c'] = sum L[a,w,a'] x[a,s,c] W[w,v,s,s'] R[c,v,c']
+ * with L = 1x1x1 ones on site 0 and R = 1x1x1 ones on site n-1 (:425-430). */
+size_t tnx_matvec1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                                   int64_t dr, int precision);
+int tnx_matvec1(const double* L, const double* W, const double* R, const double* x, double* y,
+                int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int precision,
+                void* workspace, size_t workspace_bytes, void* stream);
+
+/* Dense effective Hamiltonian H[(a,s,c),(a',s',c')] (tnpy/matrix_product_state.py:372-409),
+ * row = ket indices, column = bra indices; H has N = chi_l*d*chi_r rows. */
+int tnx_full_matrix1(const double* L, const double* W, const double* R, double* H, int64_t chi_l,
+                     int64_t d, int64_t chi_r, int64_t dl, int64_t dr, void* stream);
+
+/* diag(H_eff)[a,s,c] = sum_{w,v} L[a,w,a] W[w,v,s,s] R[c,v,c] (Davidson preconditioner). */
+int tnx_diag1(const double* L, const double* W, const double* R, double* diag, int64_t chi_l,
+              int64_t d, int64_t chi_r, int64_t dl, int64_t dr, void* stream);
+
+/* ---- environment update -------------------------------------------------------------
+ * Replaces Environment.update_left / update_right (tnpy/matrix_product_state.py:296-336).
+ * direction = +1: E_in = L_i [chi_l][dl][chi_l] -> E_out = L_{i+1} [chi_r][dr][chi_r]
+ * direction = -1: E_in = R_i [chi_r][dr][chi_r] -> E_out = R_{i-1} [chi_l][dl][chi_l] */
+size_t tnx_env_update_workspace_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r,
+                                      int64_t dl, int64_t dr, int precision);
+int tnx_env_update(int direction, const double* E_in, const double* A, const double* W,
+                   double* E_out, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                   int precision, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- lowest eigenpair of H_eff: block Davidson on the device --------------------------
+ * Replaces linalg.eigshmv -> primme.eigsh(k=1, which='SA', tol) (tnpy/linalg.py:64-87) as
+ * called by FiniteDMRG.one_site_solver (tnpy/finite_dmrg.py:97-111).
+ * x: in = start vector (need not be normalised), out = unit Ritz vector.
+ * Stops when ||H x - theta x|| <= tol, or after max_iter matvecs (TNX_ERR_NOT_CONVERGED,
+ * best Ritz pair still written). precision selects the matvec; reorthogonalisation,
+ * Rayleigh-Ritz and the final residual are FP64. With TNX_BF16X3 the returned energy and
+ * residual are recomputed with one FP64 matvec (defect correction). */
+size_t tnx_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                                     int64_t dr, int max_basis, int precision);
+int tnx_davidson1(const double* L, const double* W, const double* R, double* x, int64_t chi_l,
+                  int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter,
+                  int max_basis, int precision, double* eval_out, double* resid_out,
+                  int* iters_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- dense symmetric eigensolver (batched, one CTA per matrix) ---------------------------
+ * Replaces linalg.eigh (tnpy/linalg.py:42-61) and the np.linalg.eigh of
+ * TreeTensorNetworkSDRG.block_eigen_solver (tnpy/tsdrg.py:569-592).
+ * A: batch matrices, matrix b at A + offsets[b] (doubles), size sizes[b] (<= 1024), row-major,
+ * symmetric; destroyed. evals: batch x keep, ascending; evecs: batch x (max_size x keep)
+ * column j of matrix b = eigenvector j at evecs + b*max_size*keep, row-major [row][j].
+ * keep <= size for every matrix; rows >= size / columns >= size are left untouched. */
+size_t tnx_eigh_batched_workspace_bytes(int batch, int max_size, int keep);
+int tnx_eigh_batched(double* A, const int64_t* offsets, const int* sizes, int batch,
+                     int max_size, int keep, double* evals, double* evecs, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
+/* ---- QR / SVD gauge move -----------------------------------------------------------------
+ * Householder QR of a row-major m x n matrix (m >= n): Q (m x n, orthonormal columns),
+ * R (n x n, upper triangular). Replaces linalg.qr (tnpy/linalg.py:26-39). */
+size_t tnx_qr_workspace_bytes(int64_t m, int64_t n);
+int tnx_qr(const double* M, int64_t m, int64_t n, double* Q, double* R, void* workspace,
+           size_t workspace_bytes, void* stream);
+
+/* One-site gauge move of FiniteDMRG.sweep (tnpy/matrix_product_state.py:187-225,
+ * :359-365), QR form: direction = +1: A_site (chi_l d x chi_r) = Q R, A_site <- Q,
+ * A_next <- R A_next (A_next is chi_r x d x chi_r2). direction = -1: A_site^T = Q R,
+ * A_site <- Q^T, A_prev <- A_prev R^T (A_prev is chi_l0 x d x chi_l). The neighbour is
+ * rewritten in place; chi_other is its far bond. */
+size_t tnx_gauge_move_workspace_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r,
+                                      int64_t chi_other);
+int tnx_gauge_move(int direction, double* A_site, double* A_neighbour, int64_t chi_l,
+                   int64_t d, int64_t chi_r, int64_t chi_other, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* ---- generic helpers used by the host mirror ------------------------------------------ */
+/* C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b], row-major, FP64; trans_a / trans_b = 1
+ * means A is stored K x M / B is stored N x K. */
+int tnx_gemm_f64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                 const double* A, int64_t lda, int64_t stride_a, const double* B, int64_t ldb,
+                 int64_t stride_b, double beta, double* C, int64_t ldc, int64_t stride_c,
+                 int64_t batch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TNX_H_ */

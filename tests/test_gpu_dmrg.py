@@ -1,0 +1,66 @@
+"""fDMRG on the GPU against the CPU oracle and exact diagonalisation."""
+import numpy as np
+import pytest
+
+from oracle import dmrg as odmrg
+from oracle import ed as oed
+from oracle import models as om
+from oracle import mps as omps
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_fdmrg_case(cuda, golden):
+    """tests/test_finite_dmrg.py:9-23 of the reference: XXZ(10, 0.5), bond_dim=32, vs ED at 1e-8."""
+    import tnpy_gb300 as tg
+
+    g = golden["fdmrg_vs_ed"]
+    model = tg.model.XXZ(n=g["n"], delta=g["delta"])
+    ed = oed.ExactDiagonalization(list(model.mpo))
+    fdmrg = tg.FiniteDMRG(model.mpo, bond_dim=g["bond_dim"])
+    np.testing.assert_allclose(ed.evals[0], fdmrg.run(tol=1e-8)[-1], atol=g["atol"])
+
+
+def test_readme_spelling(cuda):
+    import tnpy_gb300 as tg
+
+    f = tg.FiniteDMRG(mpo=tg.model.XXZ(8, -0.5).mpo, chi=16)
+    e = f.update(tol=1e-8)
+    ed = oed.ExactDiagonalization(om.xxz_mpo(8, -0.5))
+    np.testing.assert_allclose(e[-1], ed.evals[0], atol=1e-8)
+    with pytest.raises(RuntimeError):
+        tg.FiniteDMRG(mpo=tg.model.XXZ(8, -0.5).mpo, chi=4).measurements
+
+
+@pytest.mark.parametrize("n,chi,seed", [(12, 32, 11), (32, 32, 1234)])
+def test_fdmrg_matches_oracle(cuda, n, chi, seed):
+    """Same seeded MPO and initial MPS: per-sweep energies agree with the CPU restatement;
+    n=12 also against ED; n=32 chi=32 is the CPU-runnable configuration."""
+    import tnpy_gb300 as tg
+
+    mpo = om.xxz_mpo(n, -0.5)
+    f = tg.FiniteDMRG(tg.MatrixProductOperator(mpo), bond_dim=chi, seed=seed, compute_variance=False)
+    e_gpu = f.run(tol=1e-10, max_sweep=10)
+    o = odmrg.FiniteDMRG(mpo, chi=chi, seed=seed)
+    e_cpu = o.run(tol=1e-10, max_sweep=10, with_variance=False)
+    assert abs(e_gpu[-1] - e_cpu[-1]) <= 1e-9 * abs(e_cpu[-1]), (e_gpu, e_cpu)
+    if n <= 12:
+        ed = oed.ExactDiagonalization(mpo)
+        np.testing.assert_allclose(e_gpu[-1], ed.evals[0], atol=1e-8)
+    sz = f.measurements.local_sz()
+    sz_ref = omps.local_sz(o.mps)
+    assert np.max(np.abs(sz - sz_ref)) < 1e-6
+
+
+def test_random_heisenberg_variance(cuda):
+    import tnpy_gb300 as tg
+
+    mpo = om.random_heisenberg_mpo(10, 1.0, seed=100)
+    f = tg.FiniteDMRG(tg.MatrixProductOperator(mpo), bond_dim=32, seed=3)
+    e = f.run(tol=1e-9, max_sweep=12)
+    ed = oed.ExactDiagonalization(mpo)
+    np.testing.assert_allclose(e[-1], ed.evals[0], atol=1e-8)
+    o = odmrg.FiniteDMRG(mpo, chi=32, seed=3)
+    o.run(tol=1e-9, max_sweep=12)
+    # the reference's variance is on the unnormalised MPS; both paths carry the same bias
+    np.testing.assert_allclose(f._variances[-1], o.variances[-1], atol=1e-6)

@@ -1,0 +1,203 @@
+"""Typed wrappers of the tnx C ABI over torch CUDA tensors.
+
+Each wrapper checks shapes on the host, takes scratch from the per-device
+workspace and calls exactly one C entry point on the current torch stream.
+Layouts follow include/tnx.h: MPS A[chi_l, d, chi_r], MPO W[dl, dr, d, d],
+environments E[chi, D, chi] (ket, mpo, bra).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import check, lib, ptr, stream_ptr, Workspace
+
+
+def _f64(t: torch.Tensor, name: str) -> torch.Tensor:
+    if t.dtype != torch.float64:
+        raise ValueError(f"{name} must be float64 (got {t.dtype})")
+    if not t.is_cuda:
+        raise ValueError(f"{name} must live on a CUDA device")
+    return t.contiguous()
+
+
+def _site_dims(L, W, R):
+    chi_l, dl, chi_l2 = L.shape
+    dl2, dr, d, d2 = W.shape
+    chi_r, dr2, chi_r2 = R.shape
+    if chi_l != chi_l2 or chi_r != chi_r2 or dl != dl2 or dr != dr2 or d != d2:
+        raise ValueError(f"inconsistent L {tuple(L.shape)}, W {tuple(W.shape)}, R {tuple(R.shape)}")
+    return chi_l, d, chi_r, dl, dr
+
+
+def precision_code(precision) -> int:
+    if isinstance(precision, int):
+        return precision
+    try:
+        return _lib.PRECISIONS[precision]
+    except KeyError:
+        raise ValueError(f"unknown precision {precision!r}; use 'fp64' or 'mixed'") from None
+
+
+def matvec1(L, W, R, x, y=None, precision="fp64"):
+    """y = H_eff x for one site (Environment.one_site_matvec, matrix_product_state.py:411-440)."""
+    L, W, R, x = (_f64(t, n) for t, n in ((L, "L"), (W, "W"), (R, "R"), (x, "x")))
+    chi_l, d, chi_r, dl, dr = _site_dims(L, W, R)
+    if x.numel() != chi_l * d * chi_r:
+        raise ValueError(f"x has {x.numel()} elements, expected {chi_l * d * chi_r}")
+    if y is None:
+        y = torch.empty((chi_l, d, chi_r), dtype=torch.float64, device=x.device)
+    p = precision_code(precision)
+    nbytes = lib.tnx_matvec1_workspace_bytes(chi_l, d, chi_r, dl, dr, p)
+    wp, wn = Workspace.get(nbytes, x.device)
+    check("tnx_matvec1", lib.tnx_matvec1(ptr(L), ptr(W), ptr(R), ptr(x), ptr(y), chi_l, d, chi_r, dl, dr,
+                                         p, wp, wn, stream_ptr()))
+    return y
+
+
+def full_matrix1(L, W, R):
+    """Dense H_eff[(a,s,c),(a',s',c')] (Environment.one_site_full_matrix, :372-409)."""
+    L, W, R = _f64(L, "L"), _f64(W, "W"), _f64(R, "R")
+    chi_l, d, chi_r, dl, dr = _site_dims(L, W, R)
+    n = chi_l * d * chi_r
+    H = torch.empty((n, n), dtype=torch.float64, device=L.device)
+    check("tnx_full_matrix1", lib.tnx_full_matrix1(ptr(L), ptr(W), ptr(R), ptr(H), chi_l, d, chi_r, dl, dr,
+                                                   stream_ptr()))
+    return H
+
+
+def diag1(L, W, R):
+    L, W, R = _f64(L, "L"), _f64(W, "W"), _f64(R, "R")
+    chi_l, d, chi_r, dl, dr = _site_dims(L, W, R)
+    out = torch.empty((chi_l, d, chi_r), dtype=torch.float64, device=L.device)
+    check("tnx_diag1", lib.tnx_diag1(ptr(L), ptr(W), ptr(R), ptr(out), chi_l, d, chi_r, dl, dr, stream_ptr()))
+    return out
+
+
+def env_update(direction: int, E, A, W, out=None, precision="fp64"):
+    """L_{i+1} from L_i (direction +1) or R_{i-1} from R_i (-1) (matrix_product_state.py:296-336)."""
+    E, A, W = _f64(E, "E"), _f64(A, "A"), _f64(W, "W")
+    chi_l, d, chi_r = A.shape
+    dl, dr = W.shape[0], W.shape[1]
+    if direction == 1:
+        if tuple(E.shape) != (chi_l, dl, chi_l):
+            raise ValueError(f"left environment {tuple(E.shape)} does not match A {tuple(A.shape)} / W")
+        shape = (chi_r, dr, chi_r)
+    elif direction == -1:
+        if tuple(E.shape) != (chi_r, dr, chi_r):
+            raise ValueError(f"right environment {tuple(E.shape)} does not match A {tuple(A.shape)} / W")
+        shape = (chi_l, dl, chi_l)
+    else:
+        raise KeyError("direction must be +1 (rightward) or -1 (leftward)")
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float64, device=A.device)
+    p = precision_code(precision)
+    nbytes = lib.tnx_env_update_workspace_bytes(direction, chi_l, d, chi_r, dl, dr, p)
+    wp, wn = Workspace.get(nbytes, A.device)
+    check("tnx_env_update", lib.tnx_env_update(direction, ptr(E), ptr(A), ptr(W), ptr(out), chi_l, d, chi_r,
+                                               dl, dr, p, wp, wn, stream_ptr()))
+    return out
+
+
+def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64", raise_on_fail=False):
+    """Lowest eigenpair of H_eff starting from x (overwritten with the unit eigenvector).
+
+    Returns (eigenvalue, residual norm, matvec count, converged)."""
+    L, W, R = _f64(L, "L"), _f64(W, "W"), _f64(R, "R")
+    if x.dtype != torch.float64 or not x.is_cuda or not x.is_contiguous():
+        raise ValueError("x must be a contiguous float64 CUDA tensor (it is overwritten)")
+    chi_l, d, chi_r, dl, dr = _site_dims(L, W, R)
+    p = precision_code(precision)
+    nbytes = lib.tnx_davidson1_workspace_bytes(chi_l, d, chi_r, dl, dr, max_basis, p)
+    wp, wn = Workspace.get(nbytes, x.device)
+    ev = ctypes.c_double(0.0)
+    rn = ctypes.c_double(0.0)
+    it = ctypes.c_int(0)
+    st = lib.tnx_davidson1(ptr(L), ptr(W), ptr(R), ptr(x), chi_l, d, chi_r, dl, dr, float(tol), int(max_iter),
+                           int(max_basis), p, ctypes.byref(ev), ctypes.byref(rn), ctypes.byref(it), wp, wn,
+                           stream_ptr())
+    converged = st == _lib.TNX_OK
+    if st != _lib.TNX_OK and (st != _lib.TNX_ERR_NOT_CONVERGED or raise_on_fail):
+        check("tnx_davidson1", st)
+    return ev.value, rn.value, it.value, converged
+
+
+def eigh_batched(mats: list[torch.Tensor], keep: int):
+    """Lowest `keep` eigenpairs of each symmetric matrix (one CTA per matrix).
+
+    Returns (evals [batch, keep], evecs [batch, max_size, keep])."""
+    if not mats:
+        raise ValueError("no matrices")
+    dev = mats[0].device
+    sizes = [int(m.shape[0]) for m in mats]
+    for m in mats:
+        if m.ndim != 2 or m.shape[0] != m.shape[1]:
+            raise ValueError(f"matrix of shape {tuple(m.shape)} is not square")
+    if keep > min(sizes):
+        raise ValueError(f"keep={keep} exceeds the smallest matrix ({min(sizes)})")
+    offs, o = [], 0
+    for s in sizes:
+        offs.append(o)
+        o += s * s
+    packed = torch.cat([_f64(m, "matrix").reshape(-1) for m in mats])
+    max_size = max(sizes)
+    batch = len(mats)
+    offsets = torch.tensor(offs, dtype=torch.int64, device=dev)
+    sizes_t = torch.tensor(sizes, dtype=torch.int32, device=dev)
+    evals = torch.empty((batch, keep), dtype=torch.float64, device=dev)
+    evecs = torch.zeros((batch, max_size, keep), dtype=torch.float64, device=dev)
+    nbytes = lib.tnx_eigh_batched_workspace_bytes(batch, max_size, keep)
+    wp, wn = Workspace.get(nbytes, dev)
+    check("tnx_eigh_batched", lib.tnx_eigh_batched(ptr(packed), ptr(offsets), ptr(sizes_t), batch, max_size,
+                                                   keep, ptr(evals), ptr(evecs), wp, wn, stream_ptr()))
+    return evals, evecs
+
+
+def qr(M: torch.Tensor):
+    """Reduced Householder QR of an m x n (m >= n) matrix."""
+    M = _f64(M, "matrix")
+    m, n = M.shape
+    Q = torch.empty((m, n), dtype=torch.float64, device=M.device)
+    Rm = torch.empty((n, n), dtype=torch.float64, device=M.device)
+    wp, wn = Workspace.get(lib.tnx_qr_workspace_bytes(m, n), M.device)
+    check("tnx_qr", lib.tnx_qr(ptr(M), m, n, ptr(Q), ptr(Rm), wp, wn, stream_ptr()))
+    return Q, Rm
+
+
+def gauge_move(direction: int, a_site: torch.Tensor, a_nb: torch.Tensor):
+    """In-place one-site gauge move (QR form of split_tensor, matrix_product_state.py:187-225)."""
+    if not (a_site.is_contiguous() and a_nb.is_contiguous()):
+        raise ValueError("MPS tensors must be contiguous")
+    chi_l, d, chi_r = a_site.shape
+    if direction == 1:
+        if a_nb.shape[0] != chi_r:
+            raise ValueError("right neighbour does not share the bond")
+        other = a_nb.shape[2]
+    elif direction == -1:
+        if a_nb.shape[2] != chi_l:
+            raise ValueError("left neighbour does not share the bond")
+        other = a_nb.shape[0]
+    else:
+        raise KeyError("MatrixProductState only supplies left or right direction.")
+    nbytes = lib.tnx_gauge_move_workspace_bytes(direction, chi_l, d, chi_r, other)
+    wp, wn = Workspace.get(nbytes, a_site.device)
+    check("tnx_gauge_move", lib.tnx_gauge_move(direction, ptr(a_site), ptr(a_nb), chi_l, d, chi_r, other, wp,
+                                               wn, stream_ptr()))
+
+
+def gemm(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False, out=None, alpha=1.0, beta=0.0):
+    a, b = _f64(a, "a"), _f64(b, "b")
+    m = a.shape[1] if trans_a else a.shape[0]
+    k = a.shape[0] if trans_a else a.shape[1]
+    n = b.shape[0] if trans_b else b.shape[1]
+    kb = b.shape[1] if trans_b else b.shape[0]
+    if k != kb:
+        raise ValueError("inner dimensions differ")
+    if out is None:
+        out = torch.zeros((m, n), dtype=torch.float64, device=a.device)
+    check("tnx_gemm_f64", lib.tnx_gemm_f64(int(trans_a), int(trans_b), m, n, k, float(alpha), ptr(a),
+                                           a.shape[1], 0, ptr(b), b.shape[1], 0, float(beta), ptr(out), n, 0, 1,
+                                           stream_ptr()))
+    return out
