@@ -129,6 +129,13 @@ int tnx_gemm_f64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, doub
                  int64_t stride_b, double beta, double* C, int64_t ldc, int64_t stride_c,
                  int64_t batch, void* stream);
 
+/* C (m x n, row-major FP64) = A (m x k) B^T (B is n x k), both row-major FP64, computed as
+ * three BF16 tensor-core products (split-BF16) with FP32 accumulation. Test / building-block
+ * entry point of the tcgen05 GEMM used by the mixed-precision matvec. */
+size_t tnx_gemm_bf16x3_workspace_bytes(int64_t m, int64_t n, int64_t k);
+int tnx_gemm_bf16x3(int64_t m, int64_t n, int64_t k, const double* A, const double* B, double* C,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,76 @@
+"""Split-BF16 tcgen05 path: the tensor-core GEMM, the mixed matvec, and the refined
+mixed-precision Davidson / fDMRG against FP64."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import dmrg as odmrg
+from oracle import models as om
+from oracle import mps as omps
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(a, dev):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (300, 260, 200), (1000, 512, 700), (5, 7, 3)])
+def test_gemm_bf16x3(cuda, m, n, k):
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(m + n + k)
+    a, b = rng.standard_normal((m, k)), rng.standard_normal((n, k))
+    c = K.gemm_bf16x3(_t(a, cuda), _t(b, cuda)).cpu().numpy()
+    ref = a @ b.T
+    # three-term split-BF16 products: ~2^-16 relative per product (plain BF16 would be ~2^-8)
+    assert np.abs(c - ref).max() <= 2e-4 * np.sqrt(k) * 0.05 + 1e-5 * np.abs(ref).max(), np.abs(c - ref).max()
+
+
+@pytest.mark.parametrize("chi_l,chi_r", [(16, 16), (64, 64), (128, 96), (256, 256)])
+def test_matvec1_mixed(cuda, chi_l, chi_r):
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(chi_l)
+    L = rng.standard_normal((chi_l, 5, chi_l))
+    R = rng.standard_normal((chi_r, 5, chi_r))
+    W = om.uniform(om.xxz_mpo(6, -0.5))[2]
+    x = rng.standard_normal((chi_l, 2, chi_r))
+    y = K.matvec1(_t(L, cuda), _t(W, cuda), _t(R, cuda), _t(x, cuda), precision="mixed").cpu().numpy()
+    ref = omps.one_site_matvec(L, W, R, x)
+    rel = np.abs(y - ref).max() / np.abs(ref).max()
+    assert rel < 1e-4, rel
+
+
+@pytest.mark.parametrize("chi", [32, 64])
+def test_davidson_mixed_defect_corrected(cuda, chi):
+    import tnpy_gb300.kernels as K
+
+    mpo = om.xxz_mpo(16, -0.5)
+    m = omps.random_mps(16, chi, 2, seed=chi)
+    env = omps.Environment(mpo, m)
+    site = 8
+    L, W, R = env.left[site], om.uniform(mpo)[site], env.right[site]
+    w = np.linalg.eigvalsh(omps.one_site_full_matrix(L, W, R))
+    x64 = _t(m[site], cuda).clone()
+    e64, *_ = K.davidson1(_t(L, cuda), _t(W, cuda), _t(R, cuda), x64, tol=1e-10)
+    xm = _t(m[site], cuda).clone()
+    em, rn, its, ok = K.davidson1(_t(L, cuda), _t(W, cuda), _t(R, cuda), xm, tol=1e-10, precision="mixed")
+    np.testing.assert_allclose(e64, w[0], rtol=1e-12)
+    # the FP64 Rayleigh quotient of the mixed eigenvector: error quadratic in the vector error
+    assert abs(em - w[0]) <= 1e-9 * abs(w[0]), (em, w[0], rn)
+
+
+def test_fdmrg_mixed_matches_fp64(cuda):
+    """XXZ(32, -0.5), chi=32: refined mixed precision within |dE|/|E| <= 1e-9 of the FP64 oracle."""
+    import tnpy_gb300 as tg
+
+    mpo = om.xxz_mpo(32, -0.5)
+    f = tg.FiniteDMRG(tg.MatrixProductOperator(mpo), bond_dim=32, seed=1234, precision="mixed",
+                      compute_variance=False)
+    e = f.run(tol=1e-10, max_sweep=10)
+    o = odmrg.FiniteDMRG(mpo, chi=32, seed=1234)
+    e_ref = o.run(tol=1e-10, max_sweep=10, with_variance=False)
+    assert abs(e[-1] - e_ref[-1]) <= 1e-9 * abs(e_ref[-1]), (e[-1], e_ref[-1])
+    sz = f.measurements.local_sz()
+    assert np.max(np.abs(sz - omps.local_sz(o.mps))) < 1e-4

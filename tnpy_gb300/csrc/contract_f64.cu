@@ -310,7 +310,8 @@ extern "C" {
 
 size_t tnx_matvec1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
                                    int precision) {
-  if (precision == TNX_BF16X3) return matvec1_bf16x3_scratch_bytes(chi_l, d, chi_r, dl, dr);
+  if (precision == TNX_BF16X3 && mixed_supported(chi_l, d, chi_r, dl, dr))
+    return matvec1_bf16x3_scratch_bytes(chi_l, d, chi_r, dl, dr);
   return 2 * align_up(size_t(matvec1_scratch_elems(chi_l, d, chi_r, dl, dr)) * sizeof(double));
 }
 
@@ -326,7 +327,9 @@ int tnx_matvec1(const double* L, const double* W, const double* R, const double*
     return TNX_ERR_WORKSPACE;
   }
   cudaStream_t st = as_stream(stream);
-  if (precision == TNX_BF16X3)
+  // sites with a bond below 16 (the chain ends) are too small for the tensor-core tiles and
+  // always run the FP64 kernels
+  if (precision == TNX_BF16X3 && mixed_supported(chi_l, d, chi_r, dl, dr))
     return matvec1_bf16x3(L, W, R, x, y, chi_l, d, chi_r, dl, dr, workspace, workspace_bytes, st);
   Arena ar(workspace, workspace_bytes);
   const int64_t ne = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);

@@ -169,7 +169,9 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
                   void* base, size_t size, DavWs* w) {
   const int64_t n = chi_l * d * chi_r;
   const int64_t ne = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);
-  const size_t mv_bytes = precision == TNX_BF16X3 ? matvec1_bf16x3_scratch_bytes(chi_l, d, chi_r, dl, dr) : 0;
+  const size_t mv_bytes = (precision == TNX_BF16X3 && mixed_supported(chi_l, d, chi_r, dl, dr))
+                              ? matvec1_bf16x3_scratch_bytes(chi_l, d, chi_r, dl, dr)
+                              : 0;
   const int nch = nchunk_for(n);
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -234,11 +236,17 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   const unsigned sblocks = (unsigned)((n + DT - 1) / DT < 152 * 8 ? (n + DT - 1) / DT : 152 * 8);
   if (mb > n) mb = int(n);
   if (mb < 2) mb = 2;
+  const bool mixed = precision == TNX_BF16X3 && w.mv != nullptr;
+  int* dflag = nullptr;
+  if (mixed) {
+    TNX_TRY(mixed_prepare(L, R, chi_l, d, chi_r, dl, dr, w.mv, st));
+    mixed_flag(w.mv, chi_l, d, chi_r, dl, dr, &dflag);
+  }
   auto matvec = [&](const double* in, double* out) -> int {
-    if (precision == TNX_BF16X3)
-      return matvec1_bf16x3(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.mv, w.mv_bytes, st);
+    if (mixed) return mixed_apply(W, in, out, chi_l, d, chi_r, dl, dr, w.mv, st);
     return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st);
   };
+  int hflag = 0;
   double* h = w.scal;               // [MAXB]
   double* nrm2 = w.scal + MAXB;     // [2]: |t|^2 before, after orthogonalisation
   double* rn2 = w.scal + MAXB + 2;  // ||r||^2
@@ -297,7 +305,12 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     TNX_LAUNCH_CHECK();
     TNX_CUDA(cudaMemcpyAsync(host, w.evals, 8, cudaMemcpyDeviceToHost, st));
     TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
+    if (dflag) TNX_CUDA(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
     TNX_CUDA(cudaStreamSynchronize(st));
+    if (hflag) {
+      set_error("tnx_davidson1: a bounded wait in the tensor-core matvec expired");
+      return TNX_ERR_TIMEOUT;
+    }
     theta = host[0];
     rnorm = sqrt(fmax(host[1], 0.0));
     if (!std::isfinite(theta) || !std::isfinite(rnorm)) {
@@ -320,7 +333,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   }
   // -- output: unit Ritz vector; FP64 Rayleigh quotient and residual for the mixed form --
   TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
-  if (precision == TNX_BF16X3) {
+  if (mixed) {
     TNX_TRY(matvec1_f64(L, W, R, w.x, w.ax, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st));
     TNX_TRY(dots(w.x, n, 1, w.ax, n, w.part, h, 1, nullptr, 0, st));
     resid_kernel<<<nch, DT, 0, st>>>(w.x, w.ax, h, n, w.part, nch);

@@ -94,6 +94,13 @@ int matvec1_bf16x3(const double* L, const double* W, const double* R, const doub
                    int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, void* scratch,
                    size_t scratch_bytes, cudaStream_t st);
 
+bool mixed_supported(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr);
+int mixed_prepare(const double* L, const double* R, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                  void* scratch, cudaStream_t st);
+int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                int64_t dr, void* scratch, cudaStream_t st);
+int mixed_flag(void* scratch, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int** flag);
+
 // ---- dense symmetric eigensolver ------------------------------------------------------
 int eigh_small_f64_ld(const double* A, const int64_t* offsets, const int* sizes, const int* lds,
                       int batch, int max_size, int keep, double* evals, double* evecs, double* work,

@@ -201,3 +201,16 @@ def gemm(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False, out=Non
                                            a.shape[1], 0, ptr(b), b.shape[1], 0, float(beta), ptr(out), n, 0, 1,
                                            stream_ptr()))
     return out
+
+
+def gemm_bf16x3(a: torch.Tensor, b: torch.Tensor):
+    """C = A B^T (A: m x k, B: n x k, FP64 in and out) on the tensor cores, split-BF16."""
+    a, b = _f64(a, "a"), _f64(b, "b")
+    m, k = a.shape
+    n, kb = b.shape
+    if k != kb:
+        raise ValueError("inner dimensions differ")
+    out = torch.empty((m, n), dtype=torch.float64, device=a.device)
+    wp, wn = Workspace.get(lib.tnx_gemm_bf16x3_workspace_bytes(m, n, k), a.device)
+    check("tnx_gemm_bf16x3", lib.tnx_gemm_bf16x3(m, n, k, ptr(a), ptr(b), ptr(out), wp, wn, stream_ptr()))
+    return out
