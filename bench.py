@@ -1,0 +1,294 @@
+#!/usr/bin/env python
+"""Benchmark: one-site fDMRG sweeps of the XXZ chain on GB300 (sweeps/s), plus the CPU
+restatement of the reference path timed on the host cores.
+
+A step is one full sweep (n-1 site updates: lowest eigenpair of the one-site effective
+Hamiltonian, 1e-5 perturbation, gauge move, environment update) of XXZ(n, delta=-0.5),
+i.e. H = sum SxSx + SySy + 0.5 SzSz, at fixed bond dimension chi, starting from a seeded
+random MPS. Environments (n * 2 * chi^2 * 5 * 8 bytes, 8.4 GB at n=100, chi=1024) are
+far larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--n 100] [--chi 1024] [--precision mixed|fp64]
+
+Under torchrun every rank runs an independent chain (replicas; a sweep does not shard),
+value = total sweeps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DMRG sweep s & matvec TFLOP/s, mixed vs FP64 GPU at |dE|<=1e-9; tSDRG realiz/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=100)
+    p.add_argument("--chi", type=int, default=1024)
+    p.add_argument("--delta", type=float, default=-0.5)
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--tol", type=float, default=1e-8)
+    p.add_argument("--seed", type=int, default=1234)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def workload(a):
+    return {"workload": f"fdmrg_onesite_xxz_n{a.n}_chi{a.chi}_{a.precision}", "model": "XXZ(n, delta=-0.5)",
+            "n": a.n, "chi": a.chi, "d": 2, "mpo_bond": 5, "precision": a.precision, "tol": a.tol,
+            "seed": a.seed, "step": "one full sweep (n-1 site updates)", "l2": "inputs > L2 (no flush)",
+            "parallelism": f"replicas{a.gpus}"}
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(gpu_index)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU sample (oracle)
+def cpu_sample(a, matvecs_per_site: float | None = None):
+    """CPU restatement of the reference's per-site work at the bench's n and chi, timed on the
+    host cores: one-site matvec (the primme callback), SVD gauge move (split_tensor) and
+    environment update, each repeated for a bounded time at a middle site of the chain.
+    A site update costs (matvecs_per_site + 1) matvecs (Davidson + perturbation) + 1 split
+    + 1 environment update; a sweep is n-1 site updates. matvecs_per_site is the average
+    the GPU run needed (20 when not given)."""
+    import numpy as np
+
+    from oracle import models as om
+    from oracle import mps as omps
+
+    n, chi = a.n, a.chi
+    site = n // 2
+    w = om.uniform(om.xxz_mpo(n, a.delta))[site]
+    rng = np.random.RandomState(a.seed)
+    dims = omps.bond_dims(n, chi, 2)
+    cl, cr = dims[site], dims[site + 1]
+    L = rng.standard_normal((cl, 5, cl))
+    R = rng.standard_normal((cr, 5, cr))
+    x = rng.standard_normal((cl, 2, cr))
+    nb = rng.standard_normal((cr, 2, dims[site + 2]))
+
+    def timed(fn, budget):
+        fn()
+        t0, k = time.perf_counter(), 0
+        while True:
+            fn()
+            k += 1
+            dt = time.perf_counter() - t0
+            if dt > budget or k >= 50:
+                return dt / k
+
+    t_mv = timed(lambda: omps.one_site_matvec(L, w, R, x), 4.0)
+    t_split = timed(lambda: omps.split_tensor([x.copy(), nb.copy()], 0, rightward=True), 4.0)
+    t_env = timed(lambda: omps.update_left(L, x, w), 4.0)
+    mv = 20.0 if matvecs_per_site is None else float(matvecs_per_site)
+    per_site = (mv + 1.0) * t_mv + t_split + t_env
+    return {"value": 1.0 / (per_site * (n - 1)), "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"numpy/scipy FP64 restatement at site {site} of n={n}, chi={chi} (bonds {cl}x{cr}): "
+                      f"matvec {t_mv * 1e3:.1f} ms, SVD split {t_split * 1e3:.1f} ms, env update "
+                      f"{t_env * 1e3:.1f} ms, each repeated for ~4 s; site update = ({mv:.1f}+1) matvecs + "
+                      f"split + env, {n - 1} site updates per sweep (full-chi site cost for every site)",
+            "seconds_per_site": per_site, "matvecs_per_site": mv,
+            "matvec_tflops": (40 * cl * cr * max(cl, cr) + 200 * cl * cr) / t_mv / 1e12}
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cb = cpu_sample(a)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "sweeps/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random MPS, XXZ MPO)",
+            "config": workload(a), "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import tnpy_gb300 as tg
+    from tnpy_gb300._lib import lib
+    import ctypes
+
+    dev = torch.device("cuda", local)
+    mpo = tg.model.XXZ(a.n, a.delta).mpo
+    f = tg.FiniteDMRG(mpo, bond_dim=a.chi, precision=a.precision, seed=a.seed + rank, compute_variance=False,
+                      device=dev)
+    dirs = [tg.Direction.RIGHTWARD, tg.Direction.LEFTWARD]
+    step = 0
+    energies = []
+
+    def one_sweep():
+        nonlocal step
+        e = f.sweep(dirs[step % 2], tol=a.tol)
+        step += 1
+        energies.append(e)
+        return e
+
+    for _ in range(a.warmup):
+        one_sweep()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    clocks = Clocks(local)
+    barrier()
+    launches0 = lib.tnx_launch_count()
+    lib.tnx_profile_begin(0)  # tcgen05 split-BF16 GEMM
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        one_sweep()
+    ev1.record()
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = lib.tnx_launch_count() - launches0
+    n_l, tot_ms, flops, nbytes = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    lib.tnx_profile_end(ctypes.byref(n_l), ctypes.byref(tot_ms), ctypes.byref(flops), ctypes.byref(nbytes))
+    dev_ms = ev0.elapsed_time(ev1)
+    t_step = dev_ms / 1e3 / a.steps
+    if world > 1:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = world / t_step
+
+    # ---- end-to-end: MPS round-trips through pinned host memory every step
+    host = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in f.mps.tensors]
+    for h, t in zip(host, f.mps.tensors):
+        h.copy_(t)
+    h2d = sum(h.numel() * 8 for h in host)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        for h, t in zip(host, f.mps.tensors):
+            t.copy_(h, non_blocking=True)
+        e = one_sweep()
+        for h, t in zip(host, f.mps.tensors):
+            h.copy_(t, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    barrier()
+    e2e_t = (time.perf_counter() - t0) / a.steps
+    if world > 1:
+        tt = torch.tensor([e2e_t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    bf16_sust = peaks.get("bf16_tflops_sustained", 1700.0)
+    achieved = flops.value / (tot_ms.value / 1e3) / 1e12 if tot_ms.value > 0 else None
+    peak = bf16_sust / 3.0
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(f"tc_gemm_chi{a.chi}")
+    roofline = {"kernel": "bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)",
+                "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "peak_note": "of measured: bf16_tflops_sustained / 3 (three BF16 products per split-BF16 product); "
+                             "achieved counts algorithmic flops 2*M*N*K of the unsplit product",
+                "launches": n_l.value, "kernel_ms_total": tot_ms.value,
+                "share_of_step_time": (tot_ms.value / dev_ms) if dev_ms > 0 else None}
+    line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (split-bf16 tensor-core matvec, FP64 environments / eigensolver)"
+            if a.precision == "mixed" else "f64",
+            "data": "synthetic (seeded random initial MPS, XXZ MPO)", "config": workload(a),
+            "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+            "e2e": {"value": world / e2e_t, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": h2d + 8},
+            "energy_last": energies[-1], "wall_s_per_step": wall / a.steps,
+            "davidson_matvecs_total": f.stats["matvecs"]}
+    sites_per_sweep = a.n - 1
+    mv_per_site = f.stats["matvecs"] / max(1, f.stats["iterative_solves"])
+    line["davidson_matvecs_per_site"] = mv_per_site
+    if rank == 0 and world == 1 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_sample(a, mv_per_site)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

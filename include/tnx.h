@@ -47,6 +47,16 @@ int tnx_version(void);
  * 10.3 is current; 0 otherwise. */
 int tnx_device_ok(void);
 
+/* Number of kernels the library has launched in this process (all entry points). */
+long long tnx_launch_count(void);
+/* Time every launch of one kernel family with CUDA events on its stream until
+ * tnx_profile_end, which synchronises and returns the launch count, the summed device
+ * time and the summed algorithmic flops / bytes of those launches.
+ * Families: 0 tcgen05 split-BF16 GEMM, 1 FP64 GEMM, 2 Davidson vector kernels,
+ * 3 QR panel, 4 dense eigensolver, 5 other. */
+int tnx_profile_begin(int family);
+int tnx_profile_end(int* launches, double* total_ms, double* flops, double* bytes);
+
 /* ---- one-site effective Hamiltonian ------------------------------------------------
  * Replaces Environment.one_site_matvec (tnpy/matrix_product_state.py:411-440):
  *   y[a',s',c'] = sum L[a,w,a'] x[a,s,c] W[w,v,s,s'] R[c,v,c']

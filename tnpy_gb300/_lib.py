@@ -46,6 +46,9 @@ SIGNATURES = {
     "tnx_last_error": (_c.c_char_p, []),
     "tnx_version": (_int, []),
     "tnx_device_ok": (_int, []),
+    "tnx_launch_count": (_c.c_longlong, []),
+    "tnx_profile_begin": (_int, [_int]),
+    "tnx_profile_end": (_int, [_pi, _pd, _pd, _pd]),
     "tnx_matvec1_workspace_bytes": (_sz, [_i64, _i64, _i64, _i64, _i64, _int]),
     "tnx_matvec1": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _int, _vp, _sz, _vp]),
     "tnx_full_matrix1": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _vp]),

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(GB_T) gemm_f64_kernel(int64_t M, int64_t N, in
                                                      int64_t sa, const double* __restrict__ B,
                                                      int64_t ldb, int64_t sb, double beta,
                                                      double* __restrict__ C, int64_t ldc,
-                                                     int64_t sc) {
+                                                     int64_t sc, int64_t k_total) {
   __shared__ double As[GB_K][GB_M + 1];
   __shared__ double Bs[GB_K][GB_N + 1];
   const int64_t bz = blockIdx.z;
@@ -38,6 +38,11 @@ __global__ void __launch_bounds__(GB_T) gemm_f64_kernel(int64_t M, int64_t N, in
   B += bz * sb;
   C += bz * sc;
   const int64_t m0 = int64_t(blockIdx.y) * GB_M, n0 = int64_t(blockIdx.x) * GB_N;
+  // split-K mode (k_total > 0): batch index bz owns K range [bz*K, min((bz+1)*K, k_total))
+  if (k_total > 0) {
+    const int64_t rem = k_total - bz * K;
+    K = rem < K ? rem : K;
+  }
   const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
   double acc[4][4];
 #pragma unroll
@@ -113,7 +118,7 @@ __global__ void __launch_bounds__(GB_T) gemm_f64_kernel(int64_t M, int64_t N, in
 
 int gemm_f64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
              int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta,
-             double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st) {
+             double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total) {
   if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
   if (k <= 0) {
     // C = beta * C; only the beta == 0 case is used here
@@ -125,14 +130,48 @@ int gemm_f64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, co
   TNX_CHECK_SHAPE(batch <= 65535, "gemm_f64: batch %lld > 65535", (long long)batch);
   dim3 grid((unsigned)((n + GB_N - 1) / GB_N), (unsigned)((m + GB_M - 1) / GB_M), (unsigned)batch);
   TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_f64: m too large");
+  profile_mark(KF_F64_GEMM, st, true);
   if (!ta && !tb)
-    gemm_f64_kernel<false, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc);
+    gemm_f64_kernel<false, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
   else if (ta && !tb)
-    gemm_f64_kernel<true, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc);
+    gemm_f64_kernel<true, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
   else if (!ta && tb)
-    gemm_f64_kernel<false, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc);
+    gemm_f64_kernel<false, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
   else
-    gemm_f64_kernel<true, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc);
+    gemm_f64_kernel<true, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+  profile_mark(KF_F64_GEMM, st, false);
+  profile_work(KF_F64_GEMM, 2.0 * double(m) * n * k * batch, 8.0 * (double(m) * k + double(k) * n + double(m) * n) * batch);
+  TNX_LAUNCH_CHECK();
+  return TNX_OK;
+}
+
+namespace {
+// C = alpha * sum_z P[z] + beta * C (P: nsplit partial m x n row-major products)
+__global__ void splitk_reduce_kernel(const double* __restrict__ P, int nsplit, int64_t m, int64_t n, double alpha,
+                                     double beta, double* __restrict__ C, int64_t ldc) {
+  const int64_t mn = m * n;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < mn; e += int64_t(gridDim.x) * blockDim.x) {
+    double acc = 0.0;
+    for (int z = 0; z < nsplit; ++z) acc += P[z * mn + e];
+    const int64_t i = e / n, j = e % n;
+    double v = alpha * acc;
+    if (beta != 0.0) v = fma(beta, C[i * ldc + j], v);
+    C[i * ldc + j] = v;
+  }
+}
+}  // namespace
+
+int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+                    const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int nsplit, double* part,
+                    cudaStream_t st) {
+  if (nsplit <= 1) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+  const int64_t kc = (k + nsplit - 1) / nsplit;
+  nsplit = int((k + kc - 1) / kc);
+  const int64_t sa = ta ? kc * lda : kc, sb = tb ? kc : kc * ldb;
+  TNX_TRY(gemm_f64(ta, tb, m, n, kc, 1.0, A, lda, sa, B, ldb, sb, 0.0, part, n, m * n, nsplit, st, k));
+  int64_t blocks = (m * n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  splitk_reduce_kernel<<<unsigned(blocks < 1 ? 1 : blocks), 256, 0, st>>>(part, nsplit, m, n, alpha, beta, C, ldc);
   TNX_LAUNCH_CHECK();
   return TNX_OK;
 }

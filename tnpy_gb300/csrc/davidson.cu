@@ -258,6 +258,13 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   int k = 0, iters = 0, precond = 1;
   double theta = 0.0, rnorm = INFINITY;
   bool converged = false;
+  // Stagnation: the split-BF16 operand is not exactly symmetric, so the residual of the
+  // mixed operator stops falling at ~1e-5 |H| (its rounding floor); the solve ends when the
+  // residual has not improved by 10% within `patience` matvecs (the FP64 defect correction
+  // below then gives the energy). The FP64 form uses a longer patience as a safeguard.
+  double best = INFINITY;
+  int best_it = 0;
+  const int patience = mixed ? 10 : 40;
   for (;;) {
     // -- new direction t -> V[k], orthogonalised against V[0..k) twice --
     double* vk = w.V + int64_t(k) * n;
@@ -297,7 +304,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     TNX_TRY(dots(w.V, n, k + 1, avk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
     ++k;
     // -- Rayleigh-Ritz (FP64 Jacobi on the k x k projected matrix, leading dim mb) --
-    TNX_TRY(eigh_small_f64_uniform(w.Hm, k, mb, 1, w.evals, w.evecs, w.jwork, st));
+    TNX_TRY(rr_lowest_f64(w.Hm, k, mb, w.evals, w.evecs, st));
     ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, precond, w.x, w.ax, w.t, n,
                                     w.part, nch);
     TNX_LAUNCH_CHECK();
@@ -319,6 +326,13 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     }
     if (rnorm <= tol || k >= n) {
       converged = true;
+      break;
+    }
+    if (rnorm < 0.9 * best) {
+      best = rnorm;
+      best_it = iters;
+    } else if (iters - best_it >= patience) {
+      converged = mixed;  // at the mixed rounding floor: done; FP64: report non-convergence
       break;
     }
     if (iters >= max_iter) break;

@@ -196,8 +196,177 @@ int tnx_eigh_batched(double* A, const int64_t* offsets, const int* sizes, int ba
     set_error("tnx_eigh_batched: workspace %zu bytes < required %zu", workspace_bytes, need);
     return TNX_ERR_WORKSPACE;
   }
+  if (batch == 1 && keep == 1 && max_size <= 64)  // one small matrix, lowest pair: one-warp path
+    return rr_lowest_f64(A, max_size, max_size, evals, evecs, as_stream(stream));
   return eigh_small_f64(A, offsets, sizes, batch, max_size, keep, evals, evecs,
                         static_cast<double*>(workspace), as_stream(stream));
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Lowest eigenpair of a small symmetric matrix (n <= 64) with one warp.
+//
+// GB300 issues FP64 at ~2 FMA/clock/SM, so an FP64 Jacobi on one SM costs ~n^3 * sweeps
+// FP64 clocks (~100 us at n = 24). Here the Jacobi sweeps run in FP32 (64x the issue
+// rate), and the lowest eigenpair is then refined in FP64 against the FP64 matrix:
+//   s <- s - sum_{j != 0} v_j (v_j . r) / (lambda_j - theta),  r = A s - theta s,
+// which contracts the error by ~(FP32 eigenvector error) per step; three steps reach
+// FP64 accuracy for a non-degenerate lowest eigenvalue, and theta = s^T A s is FP64.
+// Used for the Davidson Rayleigh-Ritz problem and the dense effective Hamiltonians
+// of the chain ends.
+// ---------------------------------------------------------------------------------------
+namespace tnx {
+namespace {
+
+constexpr int RW_MAX = 64;
+
+__global__ void __launch_bounds__(32) rr_lowest_warp_kernel(const double* __restrict__ A, int n, int ld,
+                                                          double* __restrict__ eval, double* __restrict__ evec) {
+  extern __shared__ double sm_d[];
+  double* Ad = sm_d;                                      // n x n FP64
+  float* Af = reinterpret_cast<float*>(Ad + n * n);       // n x (n+1) FP32
+  float* Vf = Af + n * (n + 1);                           // n x (n+1) FP32
+  double* s = reinterpret_cast<double*>(Vf + n * (n + 1) + ((n * (n + 1)) & 1));  // n FP64 (8-byte aligned)
+  double* r = s + n;
+  __shared__ float cs[32], ss[32];
+  __shared__ int pp[32], qq[32];
+  const int lane = threadIdx.x;
+  const int nf = n + 1;
+  float fro = 0.f;
+  for (int e = lane; e < n * n; e += 32) {
+    const int i = e / n, j = e % n;
+    const double v = A[int64_t(i) * ld + j];
+    Ad[e] = v;
+    Af[i * nf + j] = float(v);
+    Vf[i * nf + j] = (i == j) ? 1.f : 0.f;
+    fro += float(v) * float(v);
+  }
+  for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+  fro = sqrtf(fro);
+  __syncwarp();
+  if (n > 1) {
+    const int np = n + (n & 1), npairs = np / 2;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+      int any = 0;
+      for (int rnd = 0; rnd < np - 1; ++rnd) {
+        if (lane < npairs) {
+          int p = lane == 0 ? 0 : 1 + (lane - 1 + rnd) % (np - 1);
+          int q = 1 + (np - 1 - lane - 1 + rnd) % (np - 1);
+          if (p > q) { int t = p; p = q; q = t; }
+          float c = 1.f, sn = 0.f;
+          if (q < n) {
+            const float apq = Af[p * nf + q], app = Af[p * nf + p], aqq = Af[q * nf + q];
+            if (fabsf(apq) > 1e-7f * fro && fabsf(apq) > 1e-7f * sqrtf(fabsf(app * aqq))) {
+              const float th = (aqq - app) / (2.f * apq);
+              const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(1.f + th * th));
+              c = 1.f / sqrtf(1.f + t * t);
+              sn = t * c;
+              any = 1;
+            }
+          }
+          pp[lane] = p; qq[lane] = q; cs[lane] = c; ss[lane] = sn;
+        }
+        __syncwarp();
+        if (lane < npairs && ss[lane] != 0.f) {
+          const int p = pp[lane], q = qq[lane];
+          const float c = cs[lane], sn = ss[lane];
+          for (int i = 0; i < n; ++i) {  // columns p, q
+            const float a = Af[i * nf + p], b = Af[i * nf + q];
+            Af[i * nf + p] = c * a - sn * b;
+            Af[i * nf + q] = sn * a + c * b;
+          }
+        }
+        __syncwarp();
+        if (lane < npairs && ss[lane] != 0.f) {
+          const int p = pp[lane], q = qq[lane];
+          const float c = cs[lane], sn = ss[lane];
+          for (int j = 0; j < n; ++j) {  // rows p, q; V columns p, q
+            const float a = Af[p * nf + j], b = Af[q * nf + j];
+            Af[p * nf + j] = c * a - sn * b;
+            Af[q * nf + j] = sn * a + c * b;
+            const float va = Vf[j * nf + p], vb = Vf[j * nf + q];
+            Vf[j * nf + p] = c * va - sn * vb;
+            Vf[j * nf + q] = sn * va + c * vb;
+          }
+          Af[p * nf + q] = 0.f;
+          Af[q * nf + p] = 0.f;
+        }
+        __syncwarp();
+      }
+      any = __any_sync(0xffffffffu, any);
+      if (!any) break;
+    }
+  }
+  // lowest FP32 eigenvalue
+  int imin = 0;
+  float dmin = Af[0];
+  for (int i = 1; i < n; ++i)
+    if (Af[i * nf + i] < dmin) { dmin = Af[i * nf + i]; imin = i; }
+  for (int i = lane; i < n; i += 32) s[i] = double(Vf[i * nf + imin]);
+  __syncwarp();
+  double theta = 0.0;
+  for (int step = 0; step < 4; ++step) {
+    // normalise s, r = A s, theta = s.r, r -= theta s
+    double nn = 0.0;
+    for (int i = lane; i < n; i += 32) nn += s[i] * s[i];
+    for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    const double inv = 1.0 / sqrt(nn);
+    for (int i = lane; i < n; i += 32) s[i] *= inv;
+    __syncwarp();
+    double th = 0.0;
+    for (int i = lane; i < n; i += 32) {
+      double acc = 0.0;
+      for (int j = 0; j < n; ++j) acc = fma(Ad[i * n + j], s[j], acc);
+      r[i] = acc;
+      th = fma(acc, s[i], th);
+    }
+    for (int o = 16; o > 0; o >>= 1) th += __shfl_xor_sync(0xffffffffu, th, o);
+    theta = th;
+    __syncwarp();
+    if (step == 3) break;
+    for (int i = lane; i < n; i += 32) r[i] -= theta * s[i];
+    __syncwarp();
+    // s -= sum_{j != imin} v_j (v_j . r) / (lambda_j - theta)
+    for (int j = 0; j < n; ++j) {
+      if (j == imin) continue;
+      double dot = 0.0;
+      for (int i = lane; i < n; i += 32) dot = fma(double(Vf[i * nf + j]), r[i], dot);
+      for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+      double den = double(Af[j * nf + j]) - theta;
+      const double floor = 1e-6 * (double(fro) + 1e-300);
+      if (fabs(den) < floor) continue;  // (near-)degenerate partner: stays in the eigenspace
+      const double f = dot / den;
+      for (int i = lane; i < n; i += 32) s[i] -= f * double(Vf[i * nf + j]);
+    }
+    __syncwarp();
+  }
+  if (lane == 0) eval[0] = theta;
+  for (int i = lane; i < n; i += 32) evec[i] = s[i];
+}
+
+}  // namespace
+
+size_t rr_lowest_smem(int n) {
+  return size_t(n) * n * 8 + 2 * size_t(n) * (n + 1) * 4 + 8 + 2 * size_t(n) * 8;
+}
+
+int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cudaStream_t st) {
+  if (n > RW_MAX) {
+    set_error("rr_lowest_f64: n=%d > %d", n, RW_MAX);
+    return TNX_ERR_SHAPE;
+  }
+  static bool attr = false;
+  const size_t smem = rr_lowest_smem(RW_MAX);
+  if (!attr) {
+    TNX_CUDA(cudaFuncSetAttribute(rr_lowest_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    attr = true;
+  }
+  profile_mark(KF_EIGH, st, true);
+  rr_lowest_warp_kernel<<<1, 32, rr_lowest_smem(n), st>>>(A, n, ld, eval, evec);
+  profile_mark(KF_EIGH, st, false);
+  TNX_LAUNCH_CHECK();
+  return TNX_OK;
+}
+
+}  // namespace tnx

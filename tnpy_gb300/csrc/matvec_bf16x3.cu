@@ -381,7 +381,7 @@ size_t gemm_smem_bytes() {
 template <int BN>
 int launch_gemm(const __nv_bfloat16* a_hi, const __nv_bfloat16* a_lo, const __nv_bfloat16* b_hi,
                 const __nv_bfloat16* b_lo, int M, int N, int Kp, void* out, int64_t ldc, bool out_fp64,
-                int* err_flag, cudaStream_t st) {
+                int* err_flag, cudaStream_t st, int64_t k_real = -1) {
   CUtensorMap mah, mal, mbh, mbl;
   TNX_TRY(make_map(&mah, a_hi, M, Kp, BM));
   TNX_TRY(make_map(&mal, a_lo, M, Kp, BM));
@@ -394,8 +394,13 @@ int launch_gemm(const __nv_bfloat16* a_hi, const __nv_bfloat16* a_lo, const __nv
     attr_set = true;
   }
   dim3 grid(unsigned((N + BN - 1) / BN), unsigned((M + BM - 1) / BM));
+  profile_mark(KF_TC_GEMM, st, true);
   bf16x3_gemm_kernel<BN><<<grid, GEMM_THREADS, smem, st>>>(mah, mal, mbh, mbl, M, N, Kp, out, ldc,
                                                            out_fp64 ? 1 : 0, err_flag);
+  profile_mark(KF_TC_GEMM, st, false);
+  // algorithmic work: one product of the unsplit operands (2 M N K flops)
+  profile_work(KF_TC_GEMM, 2.0 * M * N * double(k_real < 0 ? Kp : k_real),
+               2.0 * 2.0 * (double(M) + N) * Kp * 3 + double(M) * N * (out_fp64 ? 8 : 4));
   TNX_LAUNCH_CHECK();
   return TNX_OK;
 }
@@ -489,10 +494,10 @@ int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int6
   // step 1: T1 (FP32) = A1 . B1^T
   if (m.N1 >= 256)
     TNX_TRY(launch_gemm<256>(m.a1h, m.a1l, m.b1h, m.b1l, int(m.M1), int(m.N1), int(m.K1p), m.T1, m.N1, false,
-                             m.flag, st));
+                             m.flag, st, chi_l));
   else
     TNX_TRY(launch_gemm<128>(m.a1h, m.a1l, m.b1h, m.b1l, int(m.M1), int(m.N1), int(m.K1p), m.T1, m.N1, false,
-                             m.flag, st));
+                             m.flag, st, chi_l));
   // step 2: MPO contraction into the split A3 operand
   {
     int64_t total = chi_l * chi_r;
@@ -505,7 +510,7 @@ int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int6
   }
   // step 3: y (FP64) = A3 . B3^T
   TNX_TRY(launch_gemm<128>(m.a3h, m.a3l, m.b3h, m.b3l, int(m.M3), int(m.N3), int(m.K3p), y, m.N3, true, m.flag,
-                           st));
+                           st, chi_r * dr));
   return TNX_OK;
 }
 
@@ -569,9 +574,9 @@ int tnx_gemm_bf16x3(int64_t m, int64_t n, int64_t k, const double* A, const doub
   split_pad_kernel<<<152 * 4, 256, 0, st>>>(B, n, k, bh, bl, kp);
   TNX_LAUNCH_CHECK();
   if (n >= 256)
-    TNX_TRY(launch_gemm<256>(ah, al, bh, bl, int(m), int(n), int(kp), C, n, true, flag, st));
+    TNX_TRY(launch_gemm<256>(ah, al, bh, bl, int(m), int(n), int(kp), C, n, true, flag, st, k));
   else
-    TNX_TRY(launch_gemm<128>(ah, al, bh, bl, int(m), int(n), int(kp), C, n, true, flag, st));
+    TNX_TRY(launch_gemm<128>(ah, al, bh, bl, int(m), int(n), int(kp), C, n, true, flag, st, k));
   int host_flag = 0;
   TNX_CUDA(cudaMemcpyAsync(&host_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
   TNX_CUDA(cudaStreamSynchronize(st));

@@ -193,15 +193,21 @@ unsigned blocks_for(int64_t total) {
 }
 
 struct QrWs {
-  double *F, *Qc, *tau, *T, *Vp, *W1, *W2;
+  double *F, *Qc, *tau, *T, *Vp, *W1, *W2, *part;
 };
+constexpr int QR_SPLIT_MAX = 16;
+inline int qr_nsplit(int64_t k) {
+  int64_t s = (k + 255) / 256;
+  return int(s < 1 ? 1 : (s > QR_SPLIT_MAX ? QR_SPLIT_MAX : s));
+}
 
 size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off += align_up(bytes); return o; };
   const int64_t np = (n + QB - 1) / QB;
   size_t oF = take(m * n * 8), oQ = take(m * n * 8), otau = take(np * QB * 8), oT = take(np * QB * QB * 8),
-         oV = take(m * QB * 8), oW1 = take(n * QB * 8), oW2 = take(n * QB * 8);
+         oV = take(m * QB * 8), oW1 = take(n * QB * 8), oW2 = take(n * QB * 8),
+         oP = take(size_t(QR_SPLIT_MAX) * n * QB * 8);
   if (w && base) {
     char* b = static_cast<char*>(base);
     w->F = reinterpret_cast<double*>(b + oF);
@@ -211,6 +217,7 @@ size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
     w->Vp = reinterpret_cast<double*>(b + oV);
     w->W1 = reinterpret_cast<double*>(b + oW1);
     w->W2 = reinterpret_cast<double*>(b + oW2);
+    w->part = reinterpret_cast<double*>(b + oP);
   }
   return off;
 }
@@ -230,8 +237,9 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st) {
       panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, w.Vp);
       TNX_LAUNCH_CHECK();
       double* C = w.F + (j0 + nb) * m + j0;  // column-major mp x nc, ld m
-      // W1^T (nc x nb) = C^T V
-      TNX_TRY(gemm_f64(false, true, nc, nb, mp, 1.0, C, m, 0, w.Vp, mp, 0, 0.0, w.W1, nb, 0, 1, st));
+      // W1^T (nc x nb) = C^T V  (thin output, long K: split over K)
+      TNX_TRY(gemm_f64_splitk(false, true, nc, nb, mp, 1.0, C, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
+                              st));
       // W2^T = W1^T T   (T column-major nb x nb with ld QB == row-major T^T)
       TNX_TRY(gemm_f64(false, true, nc, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2, nb,
                        0, 1, st));
@@ -250,7 +258,8 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st) {
     TNX_LAUNCH_CHECK();
     double* Qs = w.Qc + j0 * m + j0;  // column-major mp x nq, ld m
     // W1^T (nq x nb) = Qs^T V
-    TNX_TRY(gemm_f64(false, true, nq, nb, mp, 1.0, Qs, m, 0, w.Vp, mp, 0, 0.0, w.W1, nb, 0, 1, st));
+    TNX_TRY(gemm_f64_splitk(false, true, nq, nb, mp, 1.0, Qs, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
+                            st));
     // W2^T = W1^T T^T  -> B = T^T: op(B)[k][n] = T[n][k] = Tcm[k*QB + n] -> row-major, ld QB
     TNX_TRY(gemm_f64(false, false, nq, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2, nb,
                      0, 1, st));

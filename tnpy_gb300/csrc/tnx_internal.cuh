@@ -39,7 +39,21 @@ void set_error(const char* fmt, ...);
     }                                                                                    \
   } while (0)
 
-#define TNX_LAUNCH_CHECK() TNX_CUDA(cudaGetLastError())
+// every kernel launch of the library goes through TNX_LAUNCH_CHECK, which also counts it
+void count_launch();
+#define TNX_LAUNCH_CHECK()       \
+  do {                           \
+    ::tnx::count_launch();       \
+    TNX_CUDA(cudaGetLastError()); \
+  } while (0)
+
+// Optional CUDA-event timing of one kernel family (enabled by tnx_profile_begin).
+enum KernelFamily { KF_TC_GEMM = 0, KF_F64_GEMM = 1, KF_VECTOR = 2, KF_QR_PANEL = 3, KF_EIGH = 4, KF_OTHER = 5,
+                    KF_COUNT = 6 };
+bool profiling(int family);
+void profile_mark(int family, cudaStream_t st, bool start);
+// algorithmic work (flops, bytes) of the launch just marked, summed while profiling
+void profile_work(int family, double flops, double bytes);
 
 #define TNX_TRY(call)                     \
   do {                                    \
@@ -68,9 +82,16 @@ struct Arena {
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
 // ---- FP64 GEMM (row-major, optional transposes, strided batch) --------------------
+// k_total > 0 selects split-K: batch z multiplies the K slice [z*k, min((z+1)*k, k_total))
 int gemm_f64(bool trans_a, bool trans_b, int64_t m, int64_t n, int64_t k, double alpha,
              const double* A, int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb,
-             double beta, double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st);
+             double beta, double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st,
+             int64_t k_total = 0);
+// C = alpha * op(A) op(B) + beta * C with K split over nsplit CTAs layers; part holds
+// nsplit * m * n doubles of partial products
+int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+                    const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int nsplit, double* part,
+                    cudaStream_t st);
 
 // ---- MPO contraction steps ---------------------------------------------------------
 // T2[(a',s'),(c,v)] = sum_{w,s} T1[(w,a'),(s,c)] W[w,v,s,s']   (left / matvec form)
@@ -108,6 +129,8 @@ int eigh_small_f64_ld(const double* A, const int64_t* offsets, const int* sizes,
 // single n x n matrix with leading dimension ld; evecs as [n][keep], work 2*n*n doubles
 int eigh_small_f64_uniform(const double* A, int n, int ld, int keep, double* evals, double* evecs,
                            double* work, cudaStream_t st);
+// lowest eigenpair of one n x n (n <= 64) matrix, one warp: FP32 Jacobi + FP64 refinement
+int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cudaStream_t st);
 int eigh_small_f64(double* A, const int64_t* offsets, const int* sizes, int batch, int max_size,
                    int keep, double* evals, double* evecs, double* work, cudaStream_t st);
 
