@@ -36,8 +36,12 @@ enum tnx_status {
 };
 
 enum tnx_precision {
-  TNX_FP64 = 0,       /* plain FP64 contractions (CUDA cores)                         */
-  TNX_BF16X3 = 1      /* split-BF16 three-term products on tcgen05, FP32 accumulation  */
+  TNX_FP64 = 0,       /* plain FP64 contractions (FP64 pipe)                                */
+  TNX_BF16X3 = 1,     /* mixed form: split-BF16 three-term matvec products on tcgen05 with FP32
+                         accumulation; environment updates, gauge moves and the defect-correction
+                         matvec in double-FP32 (TNX_DF64)                                       */
+  TNX_DF64 = 2        /* FP64-class contractions in double-FP32 arithmetic on the FP32 pipe
+                         (~2^-48 relative per product)                                          */
 };
 
 const char* tnx_status_string(int status);
@@ -107,7 +111,7 @@ int tnx_davidson1(const double* L, const double* W, const double* R, double* x, 
  * A: batch matrices, matrix b at A + offsets[b] (doubles), size sizes[b] (<= 1024), row-major,
  * symmetric; destroyed. evals: batch x keep, ascending; evecs: batch x (max_size x keep)
  * column j of matrix b = eigenvector j at evecs + b*max_size*keep, row-major [row][j].
- * keep <= size for every matrix; rows >= size / columns >= size are left untouched. */
+ * A matrix smaller than keep writes only its own eigenpairs; rows >= size are left untouched. */
 size_t tnx_eigh_batched_workspace_bytes(int batch, int max_size, int keep);
 int tnx_eigh_batched(double* A, const int64_t* offsets, const int* sizes, int batch,
                      int max_size, int keep, double* evals, double* evecs, void* workspace,
@@ -128,8 +132,25 @@ int tnx_qr(const double* M, int64_t m, int64_t n, double* Q, double* R, void* wo
 size_t tnx_gauge_move_workspace_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r,
                                       int64_t chi_other);
 int tnx_gauge_move(int direction, double* A_site, double* A_neighbour, int64_t chi_l,
-                   int64_t d, int64_t chi_r, int64_t chi_other, void* workspace,
+                   int64_t d, int64_t chi_r, int64_t chi_other, int precision, void* workspace,
                    size_t workspace_bytes, void* stream);
+
+/* ---- tSDRG ----------------------------------------------------------------------------
+ * Batched two-block Hamiltonians (TreeTensorNetworkSDRG.block_hamiltonian,
+ * tnpy/tsdrg.py:607-631): item b multiplies W1_b[0,w] (x) W2_b[w,dr2-1] over the MPO bond w:
+ *   H_b[(k1 k2),(b1 b2)] = sum_w W1_b[0,w,k1,b1] W2_b[w,dr2-1,k2,b2]
+ * w1[b] -> [dl1][D][m1][m1], w2[b] -> [D][dr2][m2][m2] (device arrays of device pointers),
+ * meta[4b..4b+3] = m1, m2, dl1, dr2; H_b is written row-major at h + h_off[b]. */
+int tnx_tsdrg_block_hamiltonian(const double* const* w1, const double* const* w2, const int* meta,
+                                int D, double* h, const int64_t* h_off, int batch, int max_m,
+                                void* stream);
+/* Batched spectrum projectors (TreeTensorNetworkSDRG.spectrum_projector, tnpy/tsdrg.py:633-669):
+ *   out_b[l,r,i,j] = sum V_b[(k1 k2),i] W1_b[l,w,k1,b1] W2_b[w,r,k2,b2] V_b[(b1 b2),j]
+ * v[b] -> [m1*m2][ldv] (kept eigenvectors in the first k columns), out[b] -> [dl1][dr2][k][k],
+ * meta[5b..5b+4] = m1, m2, dl1, dr2, k; node dimensions m1, m2, k <= 32. */
+int tnx_tsdrg_project(const double* const* w1, const double* const* w2, const double* const* v,
+                      const int* meta, int D, int ldv, double* const* out, int batch, int max_m1,
+                      int max_m2, int max_k, void* stream);
 
 /* ---- generic helpers used by the host mirror ------------------------------------------ */
 /* C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b], row-major, FP64; trans_a / trans_b = 1
@@ -138,6 +159,11 @@ int tnx_gemm_f64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, doub
                  const double* A, int64_t lda, int64_t stride_a, const double* B, int64_t ldb,
                  int64_t stride_b, double beta, double* C, int64_t ldc, int64_t stride_c,
                  int64_t batch, void* stream);
+
+/* C = alpha * op(A) op(B) + beta * C in double-FP32 arithmetic (TNX_DF64), row-major. */
+int tnx_gemm_df64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+                  int64_t ldc, void* stream);
 
 /* C (m x n, row-major FP64) = A (m x k) B^T (B is n x k), both row-major FP64, computed as
  * three BF16 tensor-core products (split-BF16) with FP32 accumulation. Test / building-block

@@ -198,3 +198,47 @@ def test_random_mps_shapes(cuda):
     for a in mps.tensors[1:]:
         got = np.tensordot(got, a.cpu().numpy(), axes=([-1], [0]))
     np.testing.assert_allclose(abs(psi.reshape(-1) @ got.reshape(-1)), 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("m,n,k,ta,tb", [(64, 128, 16, False, False), (300, 260, 1000, True, False),
+                                         (1024, 37, 513, False, True), (5, 3, 7, True, True)])
+def test_gemm_df64(cuda, m, n, k, ta, tb):
+    """Double-FP32 GEMM: FP64-class accuracy (~2^-48 per product)."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(m + k)
+    a = rng.standard_normal((k, m) if ta else (m, k))
+    b = rng.standard_normal((n, k) if tb else (k, n))
+    c = K.gemm_df64(_t(a, cuda), _t(b, cuda), trans_a=ta, trans_b=tb).cpu().numpy()
+    ref = (a.T if ta else a) @ (b.T if tb else b)
+    scale = np.abs(a).max() * np.abs(b).max() * k
+    assert np.abs(c - ref).max() <= 1e-13 * scale, np.abs(c - ref).max() / scale
+
+
+@pytest.mark.parametrize("chi_l,chi_r", [(8, 16), (64, 64), (130, 96)])
+def test_env_update_df64(cuda, chi_l, chi_r):
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(chi_l)
+    A = rng.standard_normal((chi_l, 2, chi_r))
+    W = rng.standard_normal((5, 5, 2, 2))
+    L = rng.standard_normal((chi_l, 5, chi_l))
+    R = rng.standard_normal((chi_r, 5, chi_r))
+    for direction, E, ref in ((1, L, omps.update_left(L, A, W)), (-1, R, omps.update_right(R, A, W))):
+        out = K.env_update(direction, _t(E, cuda), _t(A, cuda), _t(W, cuda), precision="df64").cpu().numpy()
+        np.testing.assert_allclose(out, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def test_gauge_move_df64(cuda):
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(11)
+    a = rng.standard_normal((64, 2, 128))
+    nb = rng.standard_normal((128, 2, 40))
+    two = np.tensordot(a, nb, axes=([2], [0]))
+    ta, tn = _t(a, cuda), _t(nb, cuda)
+    K.gauge_move(1, ta, tn, precision="mixed")
+    a2, nb2 = ta.cpu().numpy(), tn.cpu().numpy()
+    m = a2.reshape(-1, 128)
+    np.testing.assert_allclose(m.T @ m, np.eye(128), atol=1e-12)
+    np.testing.assert_allclose(np.tensordot(a2, nb2, axes=([2], [0])), two, atol=1e-11)

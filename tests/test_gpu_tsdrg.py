@@ -1,0 +1,89 @@
+"""tSDRG on the GPU against the CPU oracle, the reference's known answers and ED."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ed as oed
+from oracle import models as om
+from oracle import tsdrg as ots
+
+pytestmark = pytest.mark.gpu
+
+
+def test_block_hamiltonian_kat(cuda, golden):
+    """tests/test_tsdrg.py:116-128 of the reference (n=8, h=0, every bond)."""
+    import tnpy_gb300 as tg
+    from tnpy_gb300.tsdrg import block_hamiltonians
+
+    g = golden["tsdrg_block"]
+    w = tg.model.RandomHeisenberg(g["n"], g["h"]).mpo.device_tensors(cuda)
+    mats, _ = block_hamiltonians([(w[s], w[s + 1]) for s in range(5)], cuda)
+    for m in mats:
+        np.testing.assert_array_equal(m.cpu().numpy(), np.array(g["block_hamiltonian"]))
+
+
+def test_projector_matches_oracle(cuda):
+    from tnpy_gb300.tsdrg import project
+
+    rng = np.random.RandomState(0)
+    for dl, dr, m1, m2, k in [(1, 5, 2, 2, 4), (5, 5, 8, 2, 16), (5, 1, 32, 32, 32), (5, 5, 16, 16, 40)]:
+        w1 = rng.standard_normal((dl, 5, m1, m1))
+        w2 = rng.standard_normal((5, dr, m2, m2))
+        v = np.linalg.qr(rng.standard_normal((m1 * m2, k)))[0]
+        (out,) = project([(torch.from_numpy(w1).to(cuda), torch.from_numpy(w2).to(cuda),
+                           torch.from_numpy(np.ascontiguousarray(v)).to(cuda))], cuda)
+        ref, _ = ots.spectrum_projector(w1, w2, v)
+        np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-12 * np.abs(ref).max())
+
+
+def test_notebook_kat(cuda, golden):
+    """docs/source/notebooks/tsdrg.ipynb: RandomHeisenberg(6, 3.0, seed=2021), chi=4."""
+    import tnpy_gb300 as tg
+
+    g = golden["notebook_tsdrg"]
+    t = tg.TSDRG(tg.model.RandomHeisenberg(g["n"], g["h"], seed=g["seed"]).mpo, chi=g["chi"])
+    t.run()
+    np.testing.assert_allclose(np.sort(t.evals), g["evals"], atol=1.5e-8)
+    merges = [[n.left.node_id, n.right.node_id] for n in t.tree if not n.is_leaf]
+    old_to_new = {k: k - 1 if k >= g["n"] else k for k in range(3 * g["n"])}
+    assert merges == [[old_to_new[a], old_to_new[b]] for a, b in g["merged_pairs_old_ids"]]
+    assert t.tree.root_id == 2 * g["n"] - 2
+    with pytest.raises(RuntimeError):
+        t.tree.fuse(left_id=t.tree.root_id, right_id=0, new_id=99, data=None)
+
+
+@pytest.mark.parametrize("n,h,seed", [(4, 0.1, 0), (6, 1.0, 3), (8, 0.5, 11)])
+def test_exact_tree_vs_ed(cuda, n, h, seed):
+    import tnpy_gb300 as tg
+
+    mpo = tg.model.RandomHeisenberg(n, h, seed=seed).mpo
+    t = tg.TSDRG(mpo, chi=2**n)
+    t.run()
+    np.testing.assert_allclose(np.sort(t.evals), oed.ExactDiagonalization(list(mpo)).evals, atol=1e-10)
+    assert t.tree.n_layers >= 2
+
+
+@pytest.mark.parametrize("n,chi,seed", [(16, 8, 10000), (24, 4, 10001)])
+def test_random_coupling_chain_vs_oracle(cuda, n, chi, seed):
+    """Random-coupling Heisenberg chain: same merge order and kept spectrum as the CPU restatement."""
+    import tnpy_gb300 as tg
+
+    model = tg.model.RandomCouplingHeisenberg(n, delta=1.0, seed=seed)
+    t = tg.TSDRG(model.mpo, chi=chi)
+    t.run()
+    o = ots.TreeTensorNetworkSDRG(om.random_coupling_heisenberg_mpo(n, om.random_couplings(n, 1.0, seed)), chi).run()
+    np.testing.assert_allclose(t.evals, o.evals, atol=1e-10)
+    assert [[n_.left.node_id, n_.right.node_id, n_.node_id] for n_ in t.tree if not n_.is_leaf] == \
+        [list(m) for m in o.merges]
+
+
+def test_batched_matches_single(cuda):
+    import tnpy_gb300 as tg
+
+    seeds = [10000 + r for r in range(5)]
+    mpos = [tg.model.RandomCouplingHeisenberg(12, delta=1.0, seed=s).mpo for s in seeds]
+    b = tg.BatchedTSDRG(mpos, chi=8).run()
+    for s, ev, mg in zip(seeds, b.evals, b.merges):
+        o = ots.TreeTensorNetworkSDRG(om.random_coupling_heisenberg_mpo(12, om.random_couplings(12, 1.0, s)), 8).run()
+        np.testing.assert_allclose(ev, o.evals, atol=1e-10)
+        assert [list(m) for m in mg] == [list(m) for m in o.merges]

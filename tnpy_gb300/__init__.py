@@ -23,9 +23,10 @@ from .matrix_product_state import (  # noqa: E402
     MatrixProductStateMeasurements,
 )
 from .operators import FullHamiltonian, MatrixProductOperator, SpinOperators  # noqa: E402
+from .tsdrg import TSDRG, BatchedTSDRG, TensorTree, TreeTensorNetworkSDRG  # noqa: E402
 
 __all__ = [
     "FiniteDMRG", "Metric", "Direction", "Environment", "MatrixProductState",
     "MatrixProductStateMeasurements", "FullHamiltonian", "MatrixProductOperator", "SpinOperators",
-    "linalg", "model", "logger",
+    "linalg", "model", "logger", "TSDRG", "TreeTensorNetworkSDRG", "BatchedTSDRG", "TensorTree",
 ]

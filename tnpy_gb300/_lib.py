@@ -26,7 +26,8 @@ TNX_ERR_UNSUPPORTED = 7
 
 FP64 = 0
 BF16X3 = 1
-PRECISIONS = {"fp64": FP64, "mixed": BF16X3, "bf16x3": BF16X3}
+DF64 = 2
+PRECISIONS = {"fp64": FP64, "mixed": BF16X3, "bf16x3": BF16X3, "df64": DF64}
 
 if not _LIB_PATH.exists():
     raise ImportError(
@@ -63,9 +64,12 @@ SIGNATURES = {
     "tnx_qr_workspace_bytes": (_sz, [_i64, _i64]),
     "tnx_qr": (_int, [_vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
     "tnx_gauge_move_workspace_bytes": (_sz, [_int, _i64, _i64, _i64, _i64]),
-    "tnx_gauge_move": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _vp, _sz, _vp]),
+    "tnx_gauge_move": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _int, _vp, _sz, _vp]),
+    "tnx_gemm_df64": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _vp, _i64, _dbl, _vp, _i64, _vp]),
     "tnx_gemm_bf16x3_workspace_bytes": (_sz, [_i64, _i64, _i64]),
     "tnx_gemm_bf16x3": (_int, [_i64, _i64, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "tnx_tsdrg_block_hamiltonian": (_int, [_vp, _vp, _vp, _int, _vp, _vp, _int, _int, _vp]),
+    "tnx_tsdrg_project": (_int, [_vp, _vp, _vp, _vp, _int, _int, _vp, _int, _int, _int, _int, _vp]),
     "tnx_gemm_f64": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _i64, _vp, _i64, _i64, _dbl,
                             _vp, _i64, _i64, _i64, _vp]),
 }

@@ -163,12 +163,12 @@ __global__ void splitk_reduce_kernel(const double* __restrict__ P, int nsplit, i
 
 int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
                     const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int nsplit, double* part,
-                    cudaStream_t st) {
-  if (nsplit <= 1) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+                    cudaStream_t st, bool df) {
+  if (nsplit <= 1) return gemm_fp64_class(df, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
   const int64_t kc = (k + nsplit - 1) / nsplit;
   nsplit = int((k + kc - 1) / kc);
   const int64_t sa = ta ? kc * lda : kc, sb = tb ? kc : kc * ldb;
-  TNX_TRY(gemm_f64(ta, tb, m, n, kc, 1.0, A, lda, sa, B, ldb, sb, 0.0, part, n, m * n, nsplit, st, k));
+  TNX_TRY(gemm_fp64_class(df, ta, tb, m, n, kc, 1.0, A, lda, sa, B, ldb, sb, 0.0, part, n, m * n, nsplit, st, k));
   int64_t blocks = (m * n + 255) / 256;
   if (blocks > 152 * 8) blocks = 152 * 8;
   splitk_reduce_kernel<<<unsigned(blocks < 1 ? 1 : blocks), 256, 0, st>>>(part, nsplit, m, n, alpha, beta, C, ldc);
@@ -272,14 +272,14 @@ int64_t matvec1_scratch_elems(int64_t chi_l, int64_t d, int64_t chi_r, int64_t d
 
 int matvec1_f64(const double* L, const double* W, const double* R, const double* x, double* y,
                 int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double* T1,
-                double* T2, cudaStream_t st) {
+                double* T2, cudaStream_t st, bool df) {
   // T1[(w,a'),(s,c)] = sum_a L[a,(w,a')] x[a,(s,c)]
-  TNX_TRY(gemm_f64(true, false, dl * chi_l, d * chi_r, chi_l, 1.0, L, dl * chi_l, 0, x, d * chi_r, 0,
-                   0.0, T1, d * chi_r, 0, 1, st));
+  TNX_TRY(gemm_fp64_class(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, L, dl * chi_l, 0, x, d * chi_r, 0,
+                          0.0, T1, d * chi_r, 0, 1, st));
   TNX_TRY(wcontract_left(T1, W, T2, chi_l, d, chi_r, dl, dr, st));
   // y[(a',s'),c'] = sum_{(c,v)} T2[(a',s'),(c,v)] R[(c,v),c']
-  TNX_TRY(gemm_f64(false, false, chi_l * d, chi_r, chi_r * dr, 1.0, T2, chi_r * dr, 0, R, chi_r, 0,
-                   0.0, y, chi_r, 0, 1, st));
+  TNX_TRY(gemm_fp64_class(df, false, false, chi_l * d, chi_r, chi_r * dr, 1.0, T2, chi_r * dr, 0, R, chi_r, 0,
+                          0.0, y, chi_r, 0, 1, st));
   return TNX_OK;
 }
 
@@ -359,7 +359,7 @@ int tnx_matvec1(const double* L, const double* W, const double* R, const double*
                 void* workspace, size_t workspace_bytes, void* stream) {
   TNX_TRY(check_site(L, W, R, chi_l, d, chi_r, dl, dr));
   TNX_CHECK_ARG(x && y, "null x/y pointer");
-  TNX_CHECK_ARG(precision == TNX_FP64 || precision == TNX_BF16X3, "unknown precision %d", precision);
+  TNX_CHECK_ARG(precision >= TNX_FP64 && precision <= TNX_DF64, "unknown precision %d", precision);
   size_t need = tnx_matvec1_workspace_bytes(chi_l, d, chi_r, dl, dr, precision);
   if (workspace_bytes < need || (need && !workspace)) {
     set_error("tnx_matvec1: workspace %zu bytes < required %zu", workspace_bytes, need);
@@ -374,7 +374,7 @@ int tnx_matvec1(const double* L, const double* W, const double* R, const double*
   const int64_t ne = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);
   double* T1 = ar.take<double>(ne);
   double* T2 = ar.take<double>(ne);
-  return matvec1_f64(L, W, R, x, y, chi_l, d, chi_r, dl, dr, T1, T2, st);
+  return matvec1_f64(L, W, R, x, y, chi_l, d, chi_r, dl, dr, T1, T2, st, precision == TNX_DF64);
 }
 
 int tnx_diag1(const double* L, const double* W, const double* R, double* diag, int64_t chi_l,
@@ -417,7 +417,8 @@ int tnx_env_update(int direction, const double* E_in, const double* A, const dou
   TNX_TRY(check_site(E_in, W, A, chi_l, d, chi_r, dl, dr));
   TNX_CHECK_ARG(E_out, "null E_out pointer");
   TNX_CHECK_ARG(direction == 1 || direction == -1, "direction must be +1 or -1 (got %d)", direction);
-  TNX_CHECK_ARG(precision == TNX_FP64 || precision == TNX_BF16X3, "unknown precision %d", precision);
+  TNX_CHECK_ARG(precision >= TNX_FP64 && precision <= TNX_DF64, "unknown precision %d", precision);
+  const bool df = use_df64(precision);
   size_t need = tnx_env_update_workspace_bytes(direction, chi_l, d, chi_r, dl, dr, precision);
   if (workspace_bytes < need || !workspace) {
     set_error("tnx_env_update: workspace %zu bytes < required %zu", workspace_bytes, need);
@@ -430,20 +431,20 @@ int tnx_env_update(int direction, const double* E_in, const double* A, const dou
   double* T2 = ar.take<double>(ne);
   if (direction == 1) {
     // T1[(w,a'),(s,c)] = sum_a L[a,(w,a')] A[a,(s,c)]
-    TNX_TRY(gemm_f64(true, false, dl * chi_l, d * chi_r, chi_l, 1.0, E_in, dl * chi_l, 0, A, d * chi_r,
-                     0, 0.0, T1, d * chi_r, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, E_in, dl * chi_l, 0, A, d * chi_r,
+                            0, 0.0, T1, d * chi_r, 0, 1, st));
     TNX_TRY(wcontract_left(T1, W, T2, chi_l, d, chi_r, dl, dr, st));
     // L'[(c,v),c'] = sum_{(a',s')} T2[(a',s'),(c,v)] A[(a',s'),c']
-    TNX_TRY(gemm_f64(true, false, chi_r * dr, chi_r, chi_l * d, 1.0, T2, chi_r * dr, 0, A, chi_r, 0,
-                     0.0, E_out, chi_r, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, true, false, chi_r * dr, chi_r, chi_l * d, 1.0, T2, chi_r * dr, 0, A, chi_r, 0,
+                            0.0, E_out, chi_r, 0, 1, st));
   } else {
     // T1[(a,s),(v,c')] = sum_c A[(a,s),c] R[c,(v,c')]
-    TNX_TRY(gemm_f64(false, false, chi_l * d, dr * chi_r, chi_r, 1.0, A, chi_r, 0, E_in, dr * chi_r, 0,
-                     0.0, T1, dr * chi_r, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, false, false, chi_l * d, dr * chi_r, chi_r, 1.0, A, chi_r, 0, E_in, dr * chi_r, 0,
+                            0.0, T1, dr * chi_r, 0, 1, st));
     TNX_TRY(wcontract_right(T1, W, T2, chi_l, d, chi_r, dl, dr, st));
     // R'[(a,w),a'] = sum_{(s',c')} T2[(a,w),(s',c')] A[a',(s',c')]
-    TNX_TRY(gemm_f64(false, true, chi_l * dl, chi_l, d * chi_r, 1.0, T2, d * chi_r, 0, A, d * chi_r, 0,
-                     0.0, E_out, chi_l, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, false, true, chi_l * dl, chi_l, d * chi_r, 1.0, T2, d * chi_r, 0, A, d * chi_r, 0,
+                            0.0, E_out, chi_l, 0, 1, st));
   }
   return TNX_OK;
 }

@@ -244,7 +244,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   }
   auto matvec = [&](const double* in, double* out) -> int {
     if (mixed) return mixed_apply(W, in, out, chi_l, d, chi_r, dl, dr, w.mv, st);
-    return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st);
+    return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, precision == TNX_DF64);
   };
   int hflag = 0;
   double* h = w.scal;               // [MAXB]
@@ -348,7 +348,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // -- output: unit Ritz vector; FP64 Rayleigh quotient and residual for the mixed form --
   TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
   if (mixed) {
-    TNX_TRY(matvec1_f64(L, W, R, w.x, w.ax, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st));
+    TNX_TRY(matvec1_f64(L, W, R, w.x, w.ax, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true));
     TNX_TRY(dots(w.x, n, 1, w.ax, n, w.part, h, 1, nullptr, 0, st));
     resid_kernel<<<nch, DT, 0, st>>>(w.x, w.ax, h, n, w.part, nch);
     TNX_LAUNCH_CHECK();
@@ -392,7 +392,7 @@ int tnx_davidson1(const double* L, const double* W, const double* R, double* x, 
                 max_basis);
   TNX_CHECK_ARG(max_iter >= 1, "max_iter must be >= 1");
   TNX_CHECK_ARG(tol >= 0.0, "tol must be >= 0");
-  TNX_CHECK_ARG(precision == TNX_FP64 || precision == TNX_BF16X3, "unknown precision %d", precision);
+  TNX_CHECK_ARG(precision >= TNX_FP64 && precision <= TNX_DF64, "unknown precision %d", precision);
   TNX_CHECK_SHAPE(dl * d <= 64 && dr * d <= 64, "MPO bond too large");
   return davidson1(L, W, R, x, chi_l, d, chi_r, dl, dr, tol, max_iter, max_basis, precision, eval_out,
                    resid_out, iters_out, workspace, workspace_bytes, as_stream(stream));

@@ -1,0 +1,175 @@
+// Double-FP32 ("df64") GEMM: FP64 in, FP64 out, arithmetic on the FP32 pipe.
+//
+// GB300 issues FP64 at ~2 FMA/clock/SM but FP32 at 128 FMA/clock/SM. Each FP64 operand is
+// split into a float pair (hi = fl32(x), lo = fl32(x - hi)); a product is formed as
+//   p = hi_a*hi_b, e = fma(hi_a, hi_b, -p) + hi_a*lo_b + lo_a*hi_b   (error-free + cross terms)
+// and accumulated with an error-free two-sum into a (hi, lo) float pair. About 11 FP32
+// operations per product give ~2^-48 relative accuracy per product, i.e. FP64-class
+// environments, residuals and gauge moves at several times the native FP64 rate.
+//
+// Tiling: 64 x 128 output tile per CTA, 16-deep K slab, 256 threads, 4 x 8 outputs per
+// thread at stride 16 (conflict-free shared-memory reads), operands staged as float pairs.
+#include <cuda_runtime.h>
+
+#include "tnx_internal.cuh"
+
+namespace tnx {
+namespace {
+
+constexpr int DM = 64, DN = 128, DK = 16, DT = 256;
+constexpr int RI = DM / 16, RJ = DN / 16;  // outputs per thread
+
+__device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, float& ch, float& cl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  const float s = ch + p;
+  const float bv = s - ch;
+  const float err = (ch - (s - bv)) + (p - bv);
+  ch = s;
+  cl += err + e;
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int64_t K, double alpha,
+                                                     const double* __restrict__ A, int64_t lda, int64_t sa,
+                                                     const double* __restrict__ B, int64_t ldb, int64_t sb,
+                                                     double beta, double* __restrict__ C, int64_t ldc, int64_t sc,
+                                                     int64_t k_total) {
+  __shared__ float Ah[DK][DM + 4], Al[DK][DM + 4];
+  __shared__ float Bh[DK][DN + 4], Bl[DK][DN + 4];
+  const int64_t bz = blockIdx.z;
+  A += bz * sa;
+  B += bz * sb;
+  C += bz * sc;
+  if (k_total > 0) {
+    const int64_t rem = k_total - bz * K;
+    K = rem < K ? rem : K;
+  }
+  const int64_t m0 = int64_t(blockIdx.y) * DM, n0 = int64_t(blockIdx.x) * DN;
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  float ch[RI][RJ], cl[RI][RJ];
+#pragma unroll
+  for (int i = 0; i < RI; ++i)
+#pragma unroll
+    for (int j = 0; j < RJ; ++j) ch[i][j] = cl[i][j] = 0.f;
+
+  for (int64_t k0 = 0; k0 < K; k0 += DK) {
+#pragma unroll
+    for (int r = 0; r < (DM * DK) / DT; ++r) {
+      const int e = tid + r * DT;
+      int mm, kk;
+      if (TA) {
+        mm = e % DM;
+        kk = e / DM;
+      } else {
+        kk = e % DK;
+        mm = e / DK;
+      }
+      const int64_t gm = m0 + mm, gk = k0 + kk;
+      double v = 0.0;
+      if (gm < M && gk < K) v = TA ? A[gk * lda + gm] : A[gm * lda + gk];
+      const float h = float(v);
+      Ah[kk][mm] = h;
+      Al[kk][mm] = float(v - double(h));
+    }
+#pragma unroll
+    for (int r = 0; r < (DN * DK) / DT; ++r) {
+      const int e = tid + r * DT;
+      int nn, kk;
+      if (TB) {
+        kk = e % DK;
+        nn = e / DK;
+      } else {
+        nn = e % DN;
+        kk = e / DN;
+      }
+      const int64_t gn = n0 + nn, gk = k0 + kk;
+      double v = 0.0;
+      if (gn < N && gk < K) v = TB ? B[gn * ldb + gk] : B[gk * ldb + gn];
+      const float h = float(v);
+      Bh[kk][nn] = h;
+      Bl[kk][nn] = float(v - double(h));
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < DK; ++kk) {
+      float ah[RI], al[RI], bh[RJ], bl[RJ];
+#pragma unroll
+      for (int i = 0; i < RI; ++i) {
+        ah[i] = Ah[kk][ty + 16 * i];
+        al[i] = Al[kk][ty + 16 * i];
+      }
+#pragma unroll
+      for (int j = 0; j < RJ; ++j) {
+        bh[j] = Bh[kk][tx + 16 * j];
+        bl[j] = Bl[kk][tx + 16 * j];
+      }
+#pragma unroll
+      for (int i = 0; i < RI; ++i)
+#pragma unroll
+        for (int j = 0; j < RJ; ++j) df_fma(ah[i], al[i], bh[j], bl[j], ch[i][j], cl[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < RI; ++i) {
+    const int64_t gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < RJ; ++j) {
+      const int64_t gn = n0 + tx + 16 * j;
+      if (gn >= N) continue;
+      double v = alpha * (double(ch[i][j]) + double(cl[i][j]));
+      if (beta != 0.0) v = fma(beta, C[gm * ldc + gn], v);
+      C[gm * ldc + gn] = v;
+    }
+  }
+}
+
+}  // namespace
+
+int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+              int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C, int64_t ldc, int64_t sc,
+              int64_t batch, cudaStream_t st, int64_t k_total) {
+  if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
+  if (k <= 0) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st);
+  TNX_CHECK_SHAPE(batch <= 65535, "gemm_df64: batch %lld > 65535", (long long)batch);
+  dim3 grid((unsigned)((n + DN - 1) / DN), (unsigned)((m + DM - 1) / DM), (unsigned)batch);
+  TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_df64: m too large");
+  profile_mark(KF_F64_GEMM, st, true);
+  if (!ta && !tb)
+    gemm_df64_kernel<false, false><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+  else if (ta && !tb)
+    gemm_df64_kernel<true, false><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+  else if (!ta && tb)
+    gemm_df64_kernel<false, true><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+  else
+    gemm_df64_kernel<true, true><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+  profile_mark(KF_F64_GEMM, st, false);
+  profile_work(KF_F64_GEMM, 2.0 * double(m) * n * (k_total > 0 ? k_total : k * batch),
+               8.0 * (double(m) * k + double(k) * n + double(m) * n) * batch);
+  TNX_LAUNCH_CHECK();
+  return TNX_OK;
+}
+
+int gemm_fp64_class(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                    int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C,
+                    int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total) {
+  if (df) return gemm_df64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st, k_total);
+  return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st, k_total);
+}
+
+}  // namespace tnx
+
+using namespace tnx;
+
+extern "C" int tnx_gemm_df64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                             int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                             void* stream) {
+  TNX_CHECK_ARG(A && B && C, "null pointer");
+  TNX_CHECK_ARG(m >= 0 && n >= 0 && k >= 0, "negative size");
+  return gemm_df64(trans_a != 0, trans_b != 0, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1,
+                   as_stream(stream), 0);
+}

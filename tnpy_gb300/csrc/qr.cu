@@ -225,7 +225,7 @@ size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
 }  // namespace
 
 // Factor the column-major m x n matrix in w.F (m >= n) and form Q (column-major) in w.Qc.
-int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st) {
+int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false) {
   const int64_t np = (n + QB - 1) / QB;
   for (int64_t p = 0; p < np; ++p) {
     const int64_t j0 = p * QB;
@@ -239,12 +239,12 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st) {
       double* C = w.F + (j0 + nb) * m + j0;  // column-major mp x nc, ld m
       // W1^T (nc x nb) = C^T V  (thin output, long K: split over K)
       TNX_TRY(gemm_f64_splitk(false, true, nc, nb, mp, 1.0, C, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
-                              st));
+                              st, df));
       // W2^T = W1^T T   (T column-major nb x nb with ld QB == row-major T^T)
-      TNX_TRY(gemm_f64(false, true, nc, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2, nb,
-                       0, 1, st));
+      TNX_TRY(gemm_fp64_class(df, false, true, nc, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2,
+                              nb, 0, 1, st));
       // C^T -= W2^T V^T
-      TNX_TRY(gemm_f64(false, false, nc, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, C, m, 0, 1, st));
+      TNX_TRY(gemm_fp64_class(df, false, false, nc, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, C, m, 0, 1, st));
     }
   }
   // Q = H_0 H_1 ... [I; 0]: apply panels last to first to the columns >= j0
@@ -259,12 +259,12 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st) {
     double* Qs = w.Qc + j0 * m + j0;  // column-major mp x nq, ld m
     // W1^T (nq x nb) = Qs^T V
     TNX_TRY(gemm_f64_splitk(false, true, nq, nb, mp, 1.0, Qs, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
-                            st));
+                            st, df));
     // W2^T = W1^T T^T  -> B = T^T: op(B)[k][n] = T[n][k] = Tcm[k*QB + n] -> row-major, ld QB
-    TNX_TRY(gemm_f64(false, false, nq, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2, nb,
-                     0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, false, false, nq, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2,
+                            nb, 0, 1, st));
     // Qs^T -= W2^T V^T
-    TNX_TRY(gemm_f64(false, false, nq, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, Qs, m, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, false, false, nq, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, Qs, m, 0, 1, st));
   }
   return TNX_OK;
 }
@@ -310,7 +310,9 @@ size_t tnx_gauge_move_workspace_bytes(int direction, int64_t chi_l, int64_t d, i
 }
 
 int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, int64_t d, int64_t chi_r,
-                   int64_t chi_other, void* workspace, size_t workspace_bytes, void* stream) {
+                   int64_t chi_other, int precision, void* workspace, size_t workspace_bytes, void* stream) {
+  TNX_CHECK_ARG(precision >= TNX_FP64 && precision <= TNX_DF64, "unknown precision %d", precision);
+  const bool df = use_df64(precision);
   TNX_CHECK_ARG(A_site && A_nb, "null pointer");
   TNX_CHECK_ARG(direction == 1 || direction == -1, "direction must be +1 or -1");
   TNX_CHECK_ARG(chi_l > 0 && d > 0 && chi_r > 0 && chi_other > 0, "non-positive size");
@@ -333,26 +335,26 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
     // psi (chi_l d x chi_r) row-major -> column-major
     transpose_kernel<<<dim3(unsigned((n + 31) / 32), unsigned((m + 31) / 32)), tb, 0, st>>>(A_site, m, n, w.F);
     TNX_LAUNCH_CHECK();
-    TNX_TRY(qr_colmajor(m, n, w, st));
+    TNX_TRY(qr_colmajor(m, n, w, st, df));
     transpose_kernel<<<dim3(unsigned((m + 31) / 32), unsigned((n + 31) / 32)), tb, 0, st>>>(w.Qc, n, m, A_site);
     TNX_LAUNCH_CHECK();
     extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
     TNX_LAUNCH_CHECK();
     // A_next (chi_r x d chi_other) <- R A_next
     const int64_t nc = d * chi_other;
-    TNX_TRY(gemm_f64(false, false, n, nc, n, 1.0, Rb, n, 0, A_nb, nc, 0, 0.0, tmp, nc, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, false, false, n, nc, n, 1.0, Rb, n, 0, A_nb, nc, 0, 0.0, tmp, nc, 0, 1, st));
     TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, n * nc * 8, cudaMemcpyDeviceToDevice, st));
   } else {
     // psi (chi_l x d chi_r) row-major == psi^T (d chi_r x chi_l) column-major
     TNX_CUDA(cudaMemcpyAsync(w.F, A_site, m * n * 8, cudaMemcpyDeviceToDevice, st));
-    TNX_TRY(qr_colmajor(m, n, w, st));
+    TNX_TRY(qr_colmajor(m, n, w, st, df));
     // Q column-major (d chi_r x chi_l) == Q^T row-major (chi_l x d chi_r)
     TNX_CUDA(cudaMemcpyAsync(A_site, w.Qc, m * n * 8, cudaMemcpyDeviceToDevice, st));
     extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
     TNX_LAUNCH_CHECK();
     // A_prev (chi_other d x chi_l) <- A_prev R^T
     const int64_t mr = chi_other * d;
-    TNX_TRY(gemm_f64(false, true, mr, n, n, 1.0, A_nb, n, 0, Rb, n, 0, 0.0, tmp, n, 0, 1, st));
+    TNX_TRY(gemm_fp64_class(df, false, true, mr, n, n, 1.0, A_nb, n, 0, Rb, n, 0, 0.0, tmp, n, 0, 1, st));
     TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, mr * n * 8, cudaMemcpyDeviceToDevice, st));
   }
   return TNX_OK;

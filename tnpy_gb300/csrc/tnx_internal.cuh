@@ -91,7 +91,15 @@ int gemm_f64(bool trans_a, bool trans_b, int64_t m, int64_t n, int64_t k, double
 // nsplit * m * n doubles of partial products
 int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
                     const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int nsplit, double* part,
-                    cudaStream_t st);
+                    cudaStream_t st, bool df = false);
+// double-FP32 emulated GEMM (same contract as gemm_f64)
+int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+              int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C, int64_t ldc, int64_t sc,
+              int64_t batch, cudaStream_t st, int64_t k_total = 0);
+// df = true: double-FP32 emulation; false: native FP64
+int gemm_fp64_class(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                    int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C,
+                    int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total = 0);
 
 // ---- MPO contraction steps ---------------------------------------------------------
 // T2[(a',s'),(c,v)] = sum_{w,s} T1[(w,a'),(s,c)] W[w,v,s,s']   (left / matvec form)
@@ -105,7 +113,10 @@ int wcontract_right(const double* T1, const double* W, double* T2, int64_t chi_l
 int64_t matvec1_scratch_elems(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr);
 int matvec1_f64(const double* L, const double* W, const double* R, const double* x, double* y,
                 int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double* T1,
-                double* T2, cudaStream_t st);
+                double* T2, cudaStream_t st, bool df = false);
+// FP64-class contraction selected by a precision code: TNX_FP64 -> native FP64,
+// TNX_BF16X3 / TNX_DF64 -> double-FP32 emulation
+inline bool use_df64(int precision) { return precision == TNX_BF16X3 || precision == TNX_DF64; }
 
 // Mixed-precision (split-BF16, tcgen05) matvec; returns TNX_ERR_UNSUPPORTED when the shape
 // is outside what the tensor-core kernel handles.

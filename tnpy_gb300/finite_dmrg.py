@@ -8,8 +8,9 @@ above), the 1e-5 perturbation psi += 1e-5 H_eff psi (:116-141), the gauge move
 onto the neighbour (QR form), and the environment update.
 
 ``precision='mixed'`` runs the Davidson matvecs as split-BF16 tensor-core
-contractions and recomputes each local energy with one FP64 matvec;
-environments, reorthogonalisation and Rayleigh-Ritz stay FP64.
+contractions, recomputes each local energy with one FP64-class (double-FP32)
+matvec, and runs environment updates and gauge moves in double-FP32
+arithmetic; reorthogonalisation and Rayleigh-Ritz stay FP64.
 """
 from __future__ import annotations
 
@@ -75,7 +76,7 @@ class FiniteDMRG:
         self.compute_variance = compute_variance
         if mps is None:
             mps = MatrixProductState.random(self._n_sites, self._bond_dim, self._phys_dim, seed=seed, device=device)
-        self._env = Environment(mpo=mpo, mps=mps)
+        self._env = Environment(mpo=mpo, mps=mps, precision=precision)
         self._energies = [np.nan]
         self._variances = [np.nan]
         self.sweep_seconds: list[float] = []

@@ -127,7 +127,8 @@ def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64"
 def eigh_batched(mats: list[torch.Tensor], keep: int):
     """Lowest `keep` eigenpairs of each symmetric matrix (one CTA per matrix).
 
-    Returns (evals [batch, keep], evecs [batch, max_size, keep])."""
+    Returns (evals [batch, keep], evecs [batch, max_size, keep]); for a matrix smaller than
+    `keep` only its own eigenpairs are written (the rest is NaN / zero)."""
     if not mats:
         raise ValueError("no matrices")
     dev = mats[0].device
@@ -135,8 +136,8 @@ def eigh_batched(mats: list[torch.Tensor], keep: int):
     for m in mats:
         if m.ndim != 2 or m.shape[0] != m.shape[1]:
             raise ValueError(f"matrix of shape {tuple(m.shape)} is not square")
-    if keep > min(sizes):
-        raise ValueError(f"keep={keep} exceeds the smallest matrix ({min(sizes)})")
+    if keep > max(sizes):
+        raise ValueError(f"keep={keep} exceeds the largest matrix ({max(sizes)})")
     offs, o = [], 0
     for s in sizes:
         offs.append(o)
@@ -146,7 +147,7 @@ def eigh_batched(mats: list[torch.Tensor], keep: int):
     batch = len(mats)
     offsets = torch.tensor(offs, dtype=torch.int64, device=dev)
     sizes_t = torch.tensor(sizes, dtype=torch.int32, device=dev)
-    evals = torch.empty((batch, keep), dtype=torch.float64, device=dev)
+    evals = torch.full((batch, keep), float("nan"), dtype=torch.float64, device=dev)
     evecs = torch.zeros((batch, max_size, keep), dtype=torch.float64, device=dev)
     nbytes = lib.tnx_eigh_batched_workspace_bytes(batch, max_size, keep)
     wp, wn = Workspace.get(nbytes, dev)
@@ -166,7 +167,7 @@ def qr(M: torch.Tensor):
     return Q, Rm
 
 
-def gauge_move(direction: int, a_site: torch.Tensor, a_nb: torch.Tensor):
+def gauge_move(direction: int, a_site: torch.Tensor, a_nb: torch.Tensor, precision="fp64"):
     """In-place one-site gauge move (QR form of split_tensor, matrix_product_state.py:187-225)."""
     if not (a_site.is_contiguous() and a_nb.is_contiguous()):
         raise ValueError("MPS tensors must be contiguous")
@@ -183,8 +184,8 @@ def gauge_move(direction: int, a_site: torch.Tensor, a_nb: torch.Tensor):
         raise KeyError("MatrixProductState only supplies left or right direction.")
     nbytes = lib.tnx_gauge_move_workspace_bytes(direction, chi_l, d, chi_r, other)
     wp, wn = Workspace.get(nbytes, a_site.device)
-    check("tnx_gauge_move", lib.tnx_gauge_move(direction, ptr(a_site), ptr(a_nb), chi_l, d, chi_r, other, wp,
-                                               wn, stream_ptr()))
+    check("tnx_gauge_move", lib.tnx_gauge_move(direction, ptr(a_site), ptr(a_nb), chi_l, d, chi_r, other,
+                                               precision_code(precision), wp, wn, stream_ptr()))
 
 
 def gemm(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False, out=None, alpha=1.0, beta=0.0):
@@ -213,4 +214,16 @@ def gemm_bf16x3(a: torch.Tensor, b: torch.Tensor):
     out = torch.empty((m, n), dtype=torch.float64, device=a.device)
     wp, wn = Workspace.get(lib.tnx_gemm_bf16x3_workspace_bytes(m, n, k), a.device)
     check("tnx_gemm_bf16x3", lib.tnx_gemm_bf16x3(m, n, k, ptr(a), ptr(b), ptr(out), wp, wn, stream_ptr()))
+    return out
+
+
+def gemm_df64(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False):
+    """C = op(A) op(B) in double-FP32 arithmetic (FP64 in / out)."""
+    a, b = _f64(a, "a"), _f64(b, "b")
+    m = a.shape[1] if trans_a else a.shape[0]
+    k = a.shape[0] if trans_a else a.shape[1]
+    n = b.shape[0] if trans_b else b.shape[1]
+    out = torch.empty((m, n), dtype=torch.float64, device=a.device)
+    check("tnx_gemm_df64", lib.tnx_gemm_df64(int(trans_a), int(trans_b), m, n, k, 1.0, ptr(a), a.shape[1], ptr(b),
+                                             b.shape[1], 0.0, ptr(out), n, stream_ptr()))
     return out

@@ -148,12 +148,12 @@ class MatrixProductState:
         return cls([f[k] for k in keys], device=device)
 
     # ---- gauge move ------------------------------------------------------------------
-    def split_tensor(self, site: int, direction: Direction):
+    def split_tensor(self, site: int, direction: Direction, precision="fp64"):
         """Gauge move onto the neighbour (QR form of matrix_product_state.py:187-225)."""
         if direction == Direction.RIGHTWARD:
-            K.gauge_move(1, self._t[site], self._t[site + 1])
+            K.gauge_move(1, self._t[site], self._t[site + 1], precision=precision)
         elif direction == Direction.LEFTWARD:
-            K.gauge_move(-1, self._t[site], self._t[site - 1])
+            K.gauge_move(-1, self._t[site], self._t[site - 1], precision=precision)
         else:
             raise KeyError("MatrixProductState only supplies left or right direction.")
 
@@ -191,8 +191,8 @@ class Environment:
     def __init__(self, mpo: MatrixProductOperator, mps: MatrixProductState, precision="fp64"):
         """Left / right environments of ``mps`` under ``mpo`` (matrix_product_state.py:231-250).
 
-        ``precision`` selects the contraction kernels of the environment updates; the
-        plain and the refined-mixed DMRG both keep FP64 environments."""
+        ``precision`` selects the contraction kernels of the environment updates and gauge
+        moves: 'fp64' native FP64; 'mixed' (and 'df64') FP64-class double-FP32 arithmetic."""
         if mpo.n_sites != mps.n_sites:
             raise ValueError("MPO and MPS sizes differ")
         self._mpo = mpo
@@ -266,7 +266,7 @@ class Environment:
 
     def split_tensor(self, site: int, direction: Direction):
         """:359-365."""
-        self._mps.split_tensor(site, direction)
+        self._mps.split_tensor(site, direction, precision=self.precision)
 
     def one_site_full_matrix(self, site: int) -> torch.Tensor:
         """Dense H_eff, rows = ket (:372-409)."""
