@@ -146,10 +146,10 @@ int tnx_tsdrg_block_hamiltonian(const double* const* w1, const double* const* w2
                                 void* stream);
 /* Batched spectrum projectors (TreeTensorNetworkSDRG.spectrum_projector, tnpy/tsdrg.py:633-669):
  *   out_b[l,r,i,j] = sum V_b[(k1 k2),i] W1_b[l,w,k1,b1] W2_b[w,r,k2,b2] V_b[(b1 b2),j]
- * v[b] -> [m1*m2][ldv] (kept eigenvectors in the first k columns), out[b] -> [dl1][dr2][k][k],
+ * v[b] -> [m1*m2][k] (the k kept eigenvectors as columns), out[b] -> [dl1][dr2][k][k],
  * meta[5b..5b+4] = m1, m2, dl1, dr2, k; node dimensions m1, m2, k <= 32. */
 int tnx_tsdrg_project(const double* const* w1, const double* const* w2, const double* const* v,
-                      const int* meta, int D, int ldv, double* const* out, int batch, int max_m1,
+                      const int* meta, int D, double* const* out, int batch, int max_m1,
                       int max_m2, int max_k, void* stream);
 
 /* ---- generic helpers used by the host mirror ------------------------------------------ */

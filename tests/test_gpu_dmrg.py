@@ -64,3 +64,26 @@ def test_random_heisenberg_variance(cuda):
     o.run(tol=1e-9, max_sweep=12)
     # the reference's variance is on the unnormalised MPS; both paths carry the same bias
     np.testing.assert_allclose(f._variances[-1], o.variances[-1], atol=1e-6)
+
+
+def test_bond_dimension_ramp(cuda):
+    """Enlarging the bonds leaves the state unchanged; sweeps at the larger chi lower the energy
+    towards the chi=64 oracle result."""
+    import tnpy_gb300 as tg
+    from tnpy_gb300.matrix_product_state import expectation_value
+
+    mpo = om.xxz_mpo(20, -0.5)
+    tmpo = tg.MatrixProductOperator(mpo)
+    f = tg.FiniteDMRG(tmpo, bond_dim=8, seed=2, compute_variance=False)
+    for k in range(4):
+        f.sweep(tg.Direction.RIGHTWARD if k % 2 == 0 else tg.Direction.LEFTWARD, tol=1e-10)
+    e_before = expectation_value(f.mps, tmpo) / expectation_value(f.mps)
+    f.enlarge_bond_dim(32)
+    assert max(f.mps.bond_dims()) == 32
+    e_after = expectation_value(f.mps, tmpo) / expectation_value(f.mps)
+    np.testing.assert_allclose(e_after, e_before, atol=1e-10)
+    energies = [f.sweep(tg.Direction.RIGHTWARD if k % 2 == 0 else tg.Direction.LEFTWARD, tol=1e-10) for k in range(8)]
+    o = odmrg.FiniteDMRG(mpo, chi=32, seed=2)
+    e_ref = o.run(tol=1e-10, max_sweep=12, with_variance=False)[-1]
+    assert energies[-1] < e_before - 1e-6
+    assert abs(energies[-1] - e_ref) <= 1e-7 * abs(e_ref), (energies[-1], e_ref)

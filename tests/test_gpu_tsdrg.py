@@ -63,15 +63,23 @@ def test_exact_tree_vs_ed(cuda, n, h, seed):
     assert t.tree.n_layers >= 2
 
 
+def _oracle_chain(n, seed, h):
+    fields = np.random.RandomState(seed + 1).uniform(-h, h, size=n) if h > 0 else None
+    return om.random_coupling_heisenberg_mpo(n, om.random_couplings(n, 1.0, seed), fields=fields)
+
+
+# Random fields (h > 0) break the SU(2) symmetry of the h = 0 chain: with exact multiplets
+# cut by the truncation the kept subspace is not unique and depends on the eigensolver's basis
+# inside the multiplet, so parity is checked on non-degenerate chains.
 @pytest.mark.parametrize("n,chi,seed", [(16, 8, 10000), (24, 4, 10001)])
 def test_random_coupling_chain_vs_oracle(cuda, n, chi, seed):
     """Random-coupling Heisenberg chain: same merge order and kept spectrum as the CPU restatement."""
     import tnpy_gb300 as tg
 
-    model = tg.model.RandomCouplingHeisenberg(n, delta=1.0, seed=seed)
+    model = tg.model.RandomCouplingHeisenberg(n, delta=1.0, h=0.5, seed=seed)
     t = tg.TSDRG(model.mpo, chi=chi)
     t.run()
-    o = ots.TreeTensorNetworkSDRG(om.random_coupling_heisenberg_mpo(n, om.random_couplings(n, 1.0, seed)), chi).run()
+    o = ots.TreeTensorNetworkSDRG(_oracle_chain(n, seed, 0.5), chi).run()
     np.testing.assert_allclose(t.evals, o.evals, atol=1e-10)
     assert [[n_.left.node_id, n_.right.node_id, n_.node_id] for n_ in t.tree if not n_.is_leaf] == \
         [list(m) for m in o.merges]
@@ -81,9 +89,9 @@ def test_batched_matches_single(cuda):
     import tnpy_gb300 as tg
 
     seeds = [10000 + r for r in range(5)]
-    mpos = [tg.model.RandomCouplingHeisenberg(12, delta=1.0, seed=s).mpo for s in seeds]
+    mpos = [tg.model.RandomCouplingHeisenberg(12, delta=1.0, h=0.5, seed=s).mpo for s in seeds]
     b = tg.BatchedTSDRG(mpos, chi=8).run()
     for s, ev, mg in zip(seeds, b.evals, b.merges):
-        o = ots.TreeTensorNetworkSDRG(om.random_coupling_heisenberg_mpo(12, om.random_couplings(12, 1.0, s)), 8).run()
+        o = ots.TreeTensorNetworkSDRG(_oracle_chain(12, s, 0.5), 8).run()
         np.testing.assert_allclose(ev, o.evals, atol=1e-10)
         assert [list(m) for m in mg] == [list(m) for m in o.merges]

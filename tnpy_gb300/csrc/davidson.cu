@@ -146,6 +146,41 @@ __global__ void __launch_bounds__(DT) resid_kernel(const double* __restrict__ x,
   if (threadIdx.x == 0) part[blockIdx.x] = nrm;
 }
 
+// t = ax - theta x (theta = th[0]); partial ||t||^2
+__global__ void __launch_bounds__(DT) resid_write_kernel(const double* __restrict__ x, const double* __restrict__ ax,
+                                                        const double* __restrict__ th, double* __restrict__ t,
+                                                        int64_t n, double* __restrict__ part, int nchunk) {
+  __shared__ double sh[DT / 32];
+  const double theta = th[0];
+  double nrm = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
+    const double r = ax[i] - theta * x[i];
+    t[i] = r;
+    nrm = fma(r, r, nrm);
+  }
+  nrm = block_sum(nrm, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = nrm;
+}
+
+// y = a * x + b * y with host scalars
+__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* __restrict__ y, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = fma(a, x[i], b * y[i]);
+}
+
+// out = sum_{j<k} c[j] V[j]  (host coefficients passed by value in a small struct)
+struct Coef64 {
+  double c[64];
+};
+__global__ void combine_kernel(const double* __restrict__ V, int64_t ldv, int k, Coef64 c, double* __restrict__ out,
+                               int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < k; ++j) acc = fma(c.c[j], V[int64_t(j) * ldv + i], acc);
+    out[i] = acc;
+  }
+}
+
 // after a restart to the single Ritz vector x: H = [[theta]], Ritz coefficients s = [1]
 __global__ void restart_kernel(double* Hm, const double* evals, double* evecs) {
   Hm[0] = evals[0];
@@ -265,6 +300,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   double best = INFINITY;
   int best_it = 0;
   const int patience = mixed ? 10 : 40;
+  const int max_refine = 6;  // defect-correction steps of the mixed form
   for (;;) {
     // -- new direction t -> V[k], orthogonalised against V[0..k) twice --
     double* vk = w.V + int64_t(k) * n;
@@ -345,21 +381,106 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       k = 1;
     }
   }
-  // -- output: unit Ritz vector; FP64 Rayleigh quotient and residual for the mixed form --
-  TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+  // -- output: unit Ritz vector; FP64-class Rayleigh quotient and residual for the mixed form --
   if (mixed) {
-    TNX_TRY(matvec1_f64(L, W, R, w.x, w.ax, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true));
-    TNX_TRY(dots(w.x, n, 1, w.ax, n, w.part, h, 1, nullptr, 0, st));
-    resid_kernel<<<nch, DT, 0, st>>>(w.x, w.ax, h, n, w.part, nch);
-    TNX_LAUNCH_CHECK();
-    reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
-    TNX_LAUNCH_CHECK();
-    TNX_CUDA(cudaMemcpyAsync(host, h, 8, cudaMemcpyDeviceToHost, st));
-    TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
-    TNX_CUDA(cudaStreamSynchronize(st));
-    theta = host[0];
-    rnorm = sqrt(fmax(host[1], 0.0));
+    // Defect correction. The split-BF16 operand H~ only converges the Davidson to its own
+    // eigenvector; the FP64-class residual r = H x - theta x (double-FP32 matvec) then drives
+    // Jacobi-Davidson correction steps: solve (I - x x^T)(H~ - theta)(I - x x^T) delta = -r
+    // approximately with GMRES on the tensor-core matvec, x <- (x + delta) / ||x + delta||.
+    // Each step contracts the error by about (error of H~) * ||H|| / gap.
+    double* V = w.V;    // GMRES basis (the Davidson basis is no longer needed)
+    double* Wv = w.AV;  // operator output scratch
+    const int mg = mb - 1;
+    for (int ref = 0;; ++ref) {
+      TNX_TRY(matvec1_f64(L, W, R, w.x, w.ax, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true));
+      TNX_TRY(dots(w.x, n, 1, w.ax, n, w.part, h, 1, nullptr, 0, st));
+      resid_write_kernel<<<nch, DT, 0, st>>>(w.x, w.ax, h, w.t, n, w.part, nch);
+      TNX_LAUNCH_CHECK();
+      reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
+      TNX_LAUNCH_CHECK();
+      TNX_CUDA(cudaMemcpyAsync(host, h, 8, cudaMemcpyDeviceToHost, st));
+      TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
+      TNX_CUDA(cudaStreamSynchronize(st));
+      theta = host[0];
+      rnorm = sqrt(fmax(host[1], 0.0));
+      if (rnorm <= tol || ref >= max_refine || iters >= max_iter) break;
+      // GMRES(mg) on the projected shifted operator, x0 = 0, b = -r
+      const double beta = rnorm;
+      axpby_kernel<<<sblocks, DT, 0, st>>>(-1.0 / beta, w.t, 0.0, V, n);
+      TNX_LAUNCH_CHECK();
+      double Hh[65][64] = {};
+      double cs[64], sn[64], g[65] = {};
+      g[0] = beta;
+      int j = 0;
+      for (; j < mg && iters < max_iter; ++j) {
+        double* vj = V + int64_t(j) * n;
+        double* wj = Wv + int64_t(j) * n;
+        TNX_TRY(mixed_apply(W, vj, wj, chi_l, d, chi_r, dl, dr, w.mv, st));
+        ++iters;
+        axpby_kernel<<<sblocks, DT, 0, st>>>(-theta, vj, 1.0, wj, n);
+        TNX_LAUNCH_CHECK();
+        // project out x
+        TNX_TRY(dots(w.x, n, 1, wj, n, w.part, h, 1, nullptr, 0, st));
+        update_kernel<<<nch, DT, 0, st>>>(w.x, n, 1, h, wj, n, w.part, nch);
+        TNX_LAUNCH_CHECK();
+        // Arnoldi: two classical Gram-Schmidt passes against V[0..j]
+        double hcol[65] = {};
+        for (int pass = 0; pass < 2; ++pass) {
+          TNX_TRY(dots(V, n, j + 1, wj, n, w.part, h, 1, nullptr, 0, st));
+          update_kernel<<<nch, DT, 0, st>>>(V, n, j + 1, h, wj, n, w.part, nch);
+          TNX_LAUNCH_CHECK();
+          reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, nrm2, 1, nullptr, 0);
+          TNX_LAUNCH_CHECK();
+          double hh[64];
+          TNX_CUDA(cudaMemcpyAsync(hh, h, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, st));
+          TNX_CUDA(cudaMemcpyAsync(host, nrm2, 8, cudaMemcpyDeviceToHost, st));
+          TNX_CUDA(cudaStreamSynchronize(st));
+          for (int i = 0; i <= j; ++i) hcol[i] += hh[i];
+        }
+        const double hn = sqrt(fmax(host[0], 0.0));
+        hcol[j + 1] = hn;
+        if (hn > 0.0) {
+          double* vn = V + int64_t(j + 1) * n;
+          axpby_kernel<<<sblocks, DT, 0, st>>>(1.0 / hn, wj, 0.0, vn, n);
+          TNX_LAUNCH_CHECK();
+        }
+        // apply previous Givens rotations, then a new one zeroing hcol[j+1]
+        for (int i = 0; i < j; ++i) {
+          const double a = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+          hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+          hcol[i] = a;
+        }
+        const double den = sqrt(hcol[j] * hcol[j] + hcol[j + 1] * hcol[j + 1]);
+        cs[j] = den > 0.0 ? hcol[j] / den : 1.0;
+        sn[j] = den > 0.0 ? hcol[j + 1] / den : 0.0;
+        hcol[j] = den;
+        hcol[j + 1] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        for (int i = 0; i <= j; ++i) Hh[i][j] = hcol[i];
+        if (fabs(g[j + 1]) <= 1e-3 * beta || hn == 0.0) {
+          ++j;
+          break;
+        }
+      }
+      // y = R^-1 g (upper triangular), delta = V y, x <- (x + delta) / ||x + delta||
+      Coef64 y = {};
+      for (int i = j - 1; i >= 0; --i) {
+        double t = g[i];
+        for (int q = i + 1; q < j; ++q) t -= Hh[i][q] * y.c[q];
+        y.c[i] = Hh[i][i] != 0.0 ? t / Hh[i][i] : 0.0;
+      }
+      combine_kernel<<<sblocks, DT, 0, st>>>(V, n, j, y, w.t, n);
+      TNX_LAUNCH_CHECK();
+      axpby_kernel<<<sblocks, DT, 0, st>>>(1.0, w.t, 1.0, w.x, n);
+      TNX_LAUNCH_CHECK();
+      TNX_TRY(dots(w.x, n, 1, w.x, n, w.part, nrm2, 1, nullptr, 0, st));
+      scale_kernel<<<sblocks, DT, 0, st>>>(w.x, n, nrm2);
+      TNX_LAUNCH_CHECK();
+    }
+    converged = rnorm <= tol;
   }
+  TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
   if (eval_out) *eval_out = theta;
   if (resid_out) *resid_out = rnorm;
   if (iters_out) *iters_out = iters;

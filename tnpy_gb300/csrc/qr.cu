@@ -11,15 +11,21 @@
 // factored by one CTA (reflectors + the compact-WY T factor), the trailing matrix is
 // updated with three FP64 GEMMs (W = V^T C, W = T^T W, C -= V W), and Q is formed by
 // applying the panels backwards to [I; 0].
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "tnx_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace tnx {
 namespace {
 
 constexpr int QB = 32;        // panel width
 constexpr int QT = 512;       // threads of the panel kernel
+constexpr int QC = 8;         // CTAs of the cluster panel kernel
+constexpr int QCT = 256;      // threads per CTA of the cluster panel kernel
+constexpr int QC_ROWS = 512;  // panel rows held per CTA (shared memory)
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -137,6 +143,159 @@ __global__ void __launch_bounds__(QT) panel_kernel(double* __restrict__ F, int64
   }
 }
 
+// Cluster form of panel_kernel: the panel's rows are split over QC CTAs of one thread-block
+// cluster, each holding its rows in shared memory. Per column, the partial norms and the
+// partial dot products of the reflector with the remaining columns are exchanged through
+// distributed shared memory with two cluster barriers, so the FP64 work of a panel is
+// spread over QC SMs instead of one. Every CTA combines the partials in the same order, so
+// all CTAs compute bitwise-identical reflector coefficients.
+__global__ void __cluster_dims__(QC, 1, 1) __launch_bounds__(QCT)
+    panel_cluster_kernel(double* __restrict__ F, int64_t m, int64_t j0, int nb, double* __restrict__ tau,
+                         double* __restrict__ T) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = int(cluster.block_rank());
+  extern __shared__ double pl[];  // [QB][QC_ROWS] column-major panel rows of this CTA
+  __shared__ double sig[2], alph[2], dots[2][QB];
+  __shared__ double gram[QB][QB + 1];
+  __shared__ double s_tau[QB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = QCT / 32;
+  const int64_t mp = m - j0;
+  const int64_t rpc = (mp + QC - 1) / QC;
+  const int64_t r0 = int64_t(q) * rpc;                          // first panel row of this CTA
+  const int rows = int(r0 >= mp ? 0 : (mp - r0 < rpc ? mp - r0 : rpc));
+  for (int e = tid; e < nb * rows; e += QCT) {
+    const int c = e / rows, r = e % rows;
+    pl[c * QC_ROWS + r] = F[(j0 + c) * m + j0 + r0 + r];
+  }
+  __syncthreads();
+  for (int jj = 0; jj < nb; ++jj) {
+    const int par = jj & 1;
+    const int64_t jrow = jj;  // pivot row in panel coordinates
+    // -- partial sigma over rows > pivot; the owner of the pivot row publishes alpha
+    double part = 0.0;
+    for (int r = tid; r < rows; r += QCT) {
+      const int64_t gr = r0 + r;
+      if (gr > jrow) {
+        const double x = pl[jj * QC_ROWS + r];
+        part = fma(x, x, part);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    __shared__ double red[NW];
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < NW; ++w) t += red[w];
+      sig[par] = t;
+      if (jrow >= r0 && jrow < r0 + rows) alph[par] = pl[jj * QC_ROWS + (jrow - r0)];
+    }
+    cluster.sync();
+    const int owner = int(jrow / rpc);
+    double sigma = 0.0;
+    for (int qq = 0; qq < QC; ++qq) sigma += *cluster.map_shared_rank(&sig[par], qq);
+    const double alpha = *cluster.map_shared_rank(&alph[par], owner);
+    double tj, beta, scale;
+    if (sigma == 0.0) {
+      tj = 0.0;
+      beta = alpha;
+      scale = 0.0;
+    } else {
+      const double nrm = sqrt(alpha * alpha + sigma);
+      beta = alpha >= 0.0 ? -nrm : nrm;
+      tj = (beta - alpha) / beta;
+      scale = 1.0 / (alpha - beta);
+    }
+    // -- reflector v in place (v_pivot = 1 implicit; the pivot slot keeps beta = R_jj)
+    if (tj != 0.0)
+      for (int r = tid; r < rows; r += QCT)
+        if (r0 + r > jrow) pl[jj * QC_ROWS + r] *= scale;
+    if (tid == 0) {
+      s_tau[jj] = tj;
+      if (jrow >= r0 && jrow < r0 + rows) pl[jj * QC_ROWS + (jrow - r0)] = beta;
+    }
+    __syncthreads();
+    // -- partial dots of v with the remaining columns (warp per column, lanes over rows)
+    const int rem = nb - jj - 1;
+    for (int c = warp; c < rem; c += NW) {
+      double acc = 0.0;
+      if (tj != 0.0)
+        for (int r = lane; r < rows; r += 32) {
+          const int64_t gr = r0 + r;
+          if (gr < jrow) continue;
+          const double vi = gr == jrow ? 1.0 : pl[jj * QC_ROWS + r];
+          acc = fma(vi, pl[(jj + 1 + c) * QC_ROWS + r], acc);
+        }
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) dots[par][c] = acc;
+    }
+    cluster.sync();
+    if (tj != 0.0 && rem > 0) {
+      __shared__ double wv[QB];
+      if (tid < rem) {
+        double t = 0.0;
+        for (int qq = 0; qq < QC; ++qq) t += *cluster.map_shared_rank(&dots[par][tid], qq);
+        wv[tid] = tj * t;
+      }
+      __syncthreads();
+      for (int e = tid; e < rem * rows; e += QCT) {
+        const int c = e / rows, r = e % rows;
+        const int64_t gr = r0 + r;
+        if (gr < jrow) continue;
+        const double vi = gr == jrow ? 1.0 : pl[jj * QC_ROWS + r];
+        pl[(jj + 1 + c) * QC_ROWS + r] -= wv[c] * vi;
+      }
+    }
+    __syncthreads();
+  }
+  // -- partial Gram of the reflectors, G[a][b] = v_a . v_b (a < b), reduced on rank 0
+  for (int pr = warp; pr < nb * nb; pr += NW) {
+    const int a = pr / nb, b = pr % nb;
+    if (a >= b) continue;
+    double acc = 0.0;
+    for (int r = lane; r < rows; r += 32) {
+      const int64_t gr = r0 + r;
+      if (gr < b) continue;
+      const double va = pl[a * QC_ROWS + r];  // gr >= b > a: stored part of v_a
+      const double vb = gr == b ? 1.0 : pl[b * QC_ROWS + r];
+      acc = fma(va, vb, acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) gram[a][b] = acc;
+  }
+  cluster.sync();
+  if (q == 0 && tid == 0) {
+    double G[QB][QB];
+    for (int a = 0; a < nb; ++a)
+      for (int b = a + 1; b < nb; ++b) {
+        double t = 0.0;
+        for (int qq = 0; qq < QC; ++qq) t += cluster.map_shared_rank(&gram[0][0], qq)[a * (QB + 1) + b];
+        G[a][b] = t;
+      }
+    for (int b = 0; b < nb; ++b) {
+      const double tb = s_tau[b];
+      tau[b] = tb;
+      for (int a = 0; a < b; ++a) {
+        double t = 0.0;
+        for (int c = a; c < b; ++c) t += T[c * QB + a] * G[c][b];
+        T[b * QB + a] = -tb * t;
+      }
+      T[b * QB + b] = tb;
+      for (int a = b + 1; a < QB; ++a) T[b * QB + a] = 0.0;
+    }
+    for (int b = nb; b < QB; ++b)
+      for (int a = 0; a < QB; ++a) T[b * QB + a] = 0.0;
+  }
+  // write the factored rows back; the last barrier keeps every CTA's shared memory alive
+  // until rank 0 has read the Gram partials
+  for (int e = tid; e < nb * rows; e += QCT) {
+    const int c = e / rows, r = e % rows;
+    F[(j0 + c) * m + j0 + r0 + r] = pl[c * QC_ROWS + r];
+  }
+  cluster.sync();
+}
+
 // dst (row-major rows x cols) <-> col-major transposed copy
 __global__ void transpose_kernel(const double* __restrict__ src, int64_t rows, int64_t cols,
                                  double* __restrict__ dst) {
@@ -230,7 +389,21 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
   for (int64_t p = 0; p < np; ++p) {
     const int64_t j0 = p * QB;
     const int nb = int(n - j0 < QB ? n - j0 : QB);
-    panel_kernel<<<1, QT, 0, st>>>(w.F, m, j0, nb, w.tau + p * QB, w.T + p * QB * QB);
+    if (m - j0 <= int64_t(QC) * QC_ROWS) {
+      static bool attr = false;
+      const size_t smem = size_t(QB) * QC_ROWS * sizeof(double);
+      if (!attr) {
+        TNX_CUDA(cudaFuncSetAttribute(panel_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        attr = true;
+      }
+      profile_mark(KF_QR_PANEL, st, true);
+      panel_cluster_kernel<<<QC, QCT, smem, st>>>(w.F, m, j0, nb, w.tau + p * QB, w.T + p * QB * QB);
+      profile_mark(KF_QR_PANEL, st, false);
+    } else {
+      profile_mark(KF_QR_PANEL, st, true);
+      panel_kernel<<<1, QT, 0, st>>>(w.F, m, j0, nb, w.tau + p * QB, w.T + p * QB * QB);
+      profile_mark(KF_QR_PANEL, st, false);
+    }
     TNX_LAUNCH_CHECK();
     const int64_t mp = m - j0, nc = n - j0 - nb;
     if (nc > 0) {

@@ -47,9 +47,10 @@ constexpr int PMAX = 32;  // m1, m2 <= 32 (the kept dimension of a tree node)
 __global__ void __launch_bounds__(256) project_kernel(const double* const* __restrict__ w1,
                                                       const double* const* __restrict__ w2,
                                                       const double* const* __restrict__ v, const int* __restrict__ meta,
-                                                      int D, int ldv, double* const* __restrict__ out) {
+                                                      int D, double* const* __restrict__ out) {
   const int b = blockIdx.x;
   const int m1 = meta[5 * b], m2 = meta[5 * b + 1], dl1 = meta[5 * b + 2], dr2 = meta[5 * b + 3], k = meta[5 * b + 4];
+  const int ldv = k;  // V_b is a contiguous [m1*m2][k] matrix
   const int l = blockIdx.y / D, r = blockIdx.y % D;
   if (l >= dl1 || r >= dr2) return;
   __shared__ double As[PMAX][PMAX + 1], Bs[PMAX][PMAX + 1], X[PMAX][PMAX + 1], T[PMAX][PMAX + 1];
@@ -118,13 +119,13 @@ int tnx_tsdrg_block_hamiltonian(const double* const* w1, const double* const* w2
 }
 
 int tnx_tsdrg_project(const double* const* w1, const double* const* w2, const double* const* v, const int* meta, int D,
-                      int ldv, double* const* out, int batch, int max_m1, int max_m2, int max_k, void* stream) {
+                      double* const* out, int batch, int max_m1, int max_m2, int max_k, void* stream) {
   TNX_CHECK_ARG(w1 && w2 && v && meta && out, "null pointer");
-  TNX_CHECK_ARG(batch >= 0 && D > 0 && ldv > 0, "bad batch / D / ldv");
+  TNX_CHECK_ARG(batch >= 0 && D > 0, "bad batch / D");
   if (batch == 0) return TNX_OK;
   TNX_CHECK_SHAPE(max_m1 <= PMAX && max_m2 <= PMAX && max_k <= PMAX,
                   "tsdrg projector supports node dimensions <= %d (got %d, %d, k=%d)", PMAX, max_m1, max_m2, max_k);
-  project_kernel<<<dim3(batch, D * D), 256, 0, as_stream(stream)>>>(w1, w2, v, meta, D, ldv, out);
+  project_kernel<<<dim3(batch, D * D), 256, 0, as_stream(stream)>>>(w1, w2, v, meta, D, out);
   TNX_LAUNCH_CHECK();
   return TNX_OK;
 }

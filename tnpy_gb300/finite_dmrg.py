@@ -137,6 +137,14 @@ class FiniteDMRG:
     def two_site_solver(self, site: int, tol: float = 1e-8, **kwargs):
         return NotImplemented
 
+    def enlarge_bond_dim(self, new_bond_dim: int, seed: int | None = 0):
+        """Grow the bond dimension to ``new_bond_dim`` (MatrixProductState.enlarge_bond_dim) and
+        rebuild the environments; call with the centre on site 0, i.e. before a rightward
+        sweep. One-site sweeps then fill the new directions (bond-dimension ramp)."""
+        self.mps.enlarge_bond_dim(new_bond_dim, seed=seed)
+        self._bond_dim = int(new_bond_dim)
+        self._env.rebuild()
+
     def perturb_wave_function(self, site: int, alpha: float = 1e-5):
         """psi += alpha H_eff psi, in place, not renormalised (finite_dmrg.py:116-141)."""
         psi = self.mps.tensors[site]

@@ -157,8 +157,36 @@ class MatrixProductState:
         else:
             raise KeyError("MatrixProductState only supplies left or right direction.")
 
-    def enlarge_bond_dim(self, new_bond_dim: int, method: str):
-        return NotImplemented
+    def enlarge_bond_dim(self, new_bond_dim: int, method: str = "random", seed: int | None = 0):
+        """Grow every bond to min(d^i, new_bond_dim, d^(n-i)) without changing the state
+        (the reference's stub, matrix_product_state.py:227-228, returns NotImplemented).
+
+        The MPS must be right-canonical with its centre on site 0 (the state after a leftward
+        sweep or ``random``). Bonds are grown from the right: site i+1 gains new rows that are
+        random directions orthogonalised (Householder QR on the device) against its existing
+        rows, and site i gains matching zero columns, so the state and the right-canonical form
+        are unchanged while one-site sweeps can populate the new directions. Used for the
+        bond-dimension ramp of one-site DMRG."""
+        if method != "random":
+            raise ValueError(f"unknown enlargement method {method!r}")
+        n, d = self.n_sites, self.phys_dim
+        target = bond_dims(n, new_bond_dim, d)
+        gen = torch.Generator(device="cpu")
+        gen.manual_seed(0 if seed is None else int(seed))
+        for i in range(n - 2, -1, -1):  # bond between sites i and i+1
+            a, b = self._t[i], self._t[i + 1]
+            old, new = b.shape[0], target[i + 1]
+            if new <= old:
+                continue
+            rows = b.reshape(old, -1)  # orthonormal rows (right-canonical)
+            extra = torch.randn(new - old, rows.shape[1], generator=gen, dtype=torch.float64).to(self.device)
+            m = torch.cat([rows, extra], 0).T.contiguous()  # (d chi_r) x new
+            q, _ = K.qr(m)
+            grown = torch.cat([rows, q[:, old:].T], 0)
+            self._t[i + 1] = grown.reshape(new, d, b.shape[2]).contiguous()
+            pad = torch.zeros(a.shape[0], d, new - old, dtype=torch.float64, device=self.device)
+            self._t[i] = torch.cat([a, pad], 2).contiguous()
+        return self
 
     def conj(self) -> "MatrixProductState":
         return MatrixProductState([t.clone() for t in self._t], device=self.device)
@@ -210,6 +238,16 @@ class Environment:
 
     def close(self):
         del self._left, self._right
+
+    def rebuild(self):
+        """Recompute every environment (after the bond dimensions changed)."""
+        one = torch.ones((1, 1, 1), dtype=torch.float64, device=self._mps.device)
+        self._left = {0: one}
+        self._right = {self._n_sites - 1: one.clone()}
+        for site in range(1, self._n_sites):
+            self.update_left(site)
+        for site in range(self._n_sites - 2, -1, -1):
+            self.update_right(site)
 
     @property
     def mpo(self) -> MatrixProductOperator:

@@ -195,15 +195,20 @@ def project(pairs_v, dev) -> list[torch.Tensor]:
             for w1, w2, v in pairs_v]
     if small:
         vs = [v.contiguous() for _, _, v in pairs_v]
-        ldv = {v.shape[1] for v in vs}
-        if len(ldv) == 1:
+        if vs:
             meta = torch.tensor([[w1.shape[2], w2.shape[2], w1.shape[0], w2.shape[1], v.shape[1]]
                                  for (w1, w2, _), v in zip(pairs_v, vs)], dtype=torch.int32, device=dev).reshape(-1)
+            # the pointer arrays must stay referenced until the launch is queued: a freed
+            # temporary could be handed to the next allocation of the same call
+            p1 = _ptr_array([p[0] for p in pairs_v], dev)
+            p2 = _ptr_array([p[1] for p in pairs_v], dev)
+            pv = _ptr_array(vs, dev)
+            po = _ptr_array(outs, dev)
             check("tnx_tsdrg_project", lib.tnx_tsdrg_project(
-                ptr(_ptr_array([p[0] for p in pairs_v], dev)), ptr(_ptr_array([p[1] for p in pairs_v], dev)),
-                ptr(_ptr_array(vs, dev)), ptr(meta), int(D), int(vs[0].shape[1]), ptr(_ptr_array(outs, dev)),
-                len(pairs_v), max(p[0].shape[2] for p in pairs_v), max(p[1].shape[2] for p in pairs_v),
-                max(v.shape[1] for v in vs), stream_ptr()))
+                ptr(p1), ptr(p2), ptr(pv), ptr(meta), int(D), ptr(po), len(pairs_v),
+                max(p[0].shape[2] for p in pairs_v), max(p[1].shape[2] for p in pairs_v), max(v.shape[1] for v in vs),
+                stream_ptr()))
+            del p1, p2, pv, po
             return outs
     # general sizes: M_lr = sum_w W1[l,w] (x) W2[w,r] by the block-Hamiltonian kernel, then two GEMMs
     for (w1, w2, v), out in zip(pairs_v, outs):
