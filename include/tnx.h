@@ -71,6 +71,21 @@ int tnx_matvec1(const double* L, const double* W, const double* R, const double*
                 int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int precision,
                 void* workspace, size_t workspace_bytes, void* stream);
 
+/* FP64 one-site matvec (same contract as tnx_matvec1 with TNX_FP64) that allocates nothing and
+ * takes no workspace: for callers that cannot allocate device memory where they call it
+ * (inside a stream capture that must not allocate, allocator-less host bindings, processes
+ * whose device memory is held by another framework's pool). Its two intermediates live in a
+ * file-scope device array of 2 x TNX_NOALLOC_MAX_ELEMS doubles (32 MiB) that every device
+ * loading the library keeps until exit. Limit: chi_l * d * chi_r * max(dl, dr) <=
+ * TNX_NOALLOC_MAX_ELEMS (e.g. chi_l = chi_r = 448 with D = 5, d = 2); larger problems return
+ * TNX_ERR_SHAPE. The first call on a device looks up the array's device address (do it before
+ * any stream capture). All calls share the array: calls that overlap on the GPU race.
+ * No counterpart in the reference. */
+#define TNX_NOALLOC_MAX_ELEMS 2097152
+int tnx_matvec1_noalloc(const double* L, const double* W, const double* R, const double* x,
+                        double* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                        void* stream);
+
 /* Dense effective Hamiltonian H[(a,s,c),(a',s',c')] (tnpy/matrix_product_state.py:372-409),
  * row = ket indices, column = bra indices; H has N = chi_l*d*chi_r rows. */
 int tnx_full_matrix1(const double* L, const double* W, const double* R, double* H, int64_t chi_l,
