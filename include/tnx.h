@@ -109,8 +109,9 @@ int tnx_env_update(int direction, const double* E_in, const double* A, const dou
  * Replaces linalg.eigshmv -> primme.eigsh(k=1, which='SA', tol) (tnpy/linalg.py:64-87) as
  * called by FiniteDMRG.one_site_solver (tnpy/finite_dmrg.py:97-111).
  * x: in = start vector (need not be normalised), out = unit Ritz vector.
- * Stops when ||H x - theta x|| <= tol, or after max_iter matvecs (TNX_ERR_NOT_CONVERGED,
- * best Ritz pair still written). precision selects the matvec; reorthogonalisation,
+ * Stops when ||H x - theta x|| <= tol * max(1, |theta|) (primme's residual criterion relative to
+ * the operator scale), or after max_iter matvecs (TNX_ERR_NOT_CONVERGED, best Ritz pair still
+ * written). precision selects the matvec; reorthogonalisation,
  * Rayleigh-Ritz and the final residual are FP64. With TNX_BF16X3 the returned energy and
  * residual are recomputed with one FP64 matvec (defect correction). */
 size_t tnx_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
@@ -166,6 +167,20 @@ int tnx_tsdrg_block_hamiltonian(const double* const* w1, const double* const* w2
 int tnx_tsdrg_project(const double* const* w1, const double* const* w2, const double* const* v,
                       const int* meta, int D, double* const* out, int batch, int max_m1,
                       int max_m2, int max_k, void* stream);
+
+/* Lowest-keep eigenpairs of tSDRG block Hamiltonians H = sum_w W1_b[0,w] (x) W2_b[w,dr2-1]
+ * (TreeTensorNetworkSDRG.block_eigen_solver, tnpy/tsdrg.py:569-592) without forming H:
+ * Chebyshev-filtered subspace iteration on the Kronecker matvec (FP32 for TNX_DF64 /
+ * TNX_BF16X3, FP64 for TNX_FP64) followed by an FP64 Rayleigh-Ritz refinement, one CTA per
+ * block. meta[5b..5b+4] = m1, m2, dr2, k, p (node dimensions m1, m2 <= 32, k kept pairs,
+ * p = subspace size with k <= p <= min(m1 m2, 48)); D <= 6; keep >= every k.
+ * evals: batch x keep; evecs: batch x (max_m x keep) row-major, like tnx_eigh_batched;
+ * iters (device, may be null): filter iterations per block. */
+size_t tnx_tsdrg_block_eigh_workspace_bytes(int batch, int max_m, int keep, int precision);
+int tnx_tsdrg_block_eigh(const double* const* w1, const double* const* w2, const int* meta, int D,
+                         int batch, int max_m, int keep, int precision, double* evals,
+                         double* evecs, int* iters, void* workspace, size_t workspace_bytes,
+                         void* stream);
 
 /* ---- generic helpers used by the host mirror ------------------------------------------ */
 /* C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b], row-major, FP64; trans_a / trans_b = 1

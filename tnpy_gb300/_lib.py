@@ -70,6 +70,8 @@ SIGNATURES = {
     "tnx_gemm_bf16x3": (_int, [_i64, _i64, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tnx_tsdrg_block_hamiltonian": (_int, [_vp, _vp, _vp, _int, _vp, _vp, _int, _int, _vp]),
     "tnx_tsdrg_project": (_int, [_vp, _vp, _vp, _vp, _int, _vp, _int, _int, _int, _int, _vp]),
+    "tnx_tsdrg_block_eigh_workspace_bytes": (_sz, [_int, _int, _int, _int]),
+    "tnx_tsdrg_block_eigh": (_int, [_vp, _vp, _vp, _int, _int, _int, _int, _int, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tnx_gemm_f64": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _i64, _vp, _i64, _i64, _dbl,
                             _vp, _i64, _i64, _i64, _vp]),
 }

@@ -162,6 +162,16 @@ __global__ void __launch_bounds__(DT) resid_write_kernel(const double* __restric
   if (threadIdx.x == 0) part[blockIdx.x] = nrm;
 }
 
+// out = in / (diag - theta), the diagonal preconditioner with its denominator kept >= 1e-2
+__global__ void precond_kernel(const double* __restrict__ in, const double* __restrict__ diag, double theta,
+                               double* __restrict__ out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    double den = diag[i] - theta;
+    if (fabs(den) < 1e-2) den = den >= 0.0 ? 1e-2 : -1e-2;
+    out[i] = in[i] / den;
+  }
+}
+
 // y = a * x + b * y with host scalars
 __global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* __restrict__ y, int64_t n) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
@@ -299,8 +309,15 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // below then gives the energy). The FP64 form uses a longer patience as a safeguard.
   double best = INFINITY;
   int best_it = 0;
-  const int patience = mixed ? 10 : 40;
+  const int patience = mixed ? 8 : 40;
   const int max_refine = 6;  // defect-correction steps of the mixed form
+  // The mixed form hands over to the FP64-class defect correction once the split-BF16 residual
+  // is below 3e-6 |theta| or has stagnated at its ~1e-5 |H| floor (an earlier hand-over can leave
+  // the Davidson on an excited state that the correction then converges to), and refines the
+  // FP64-class residual
+  // to max(tol, 2e-7) |theta|: the energy error is quadratic in the residual,
+  // ~ (2e-7 |theta|)^2 / gap, i.e. below 1e-12 |E| for local gaps above 1e-2.
+  const double mixed_handover = 3e-6, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
   for (;;) {
     // -- new direction t -> V[k], orthogonalised against V[0..k) twice --
     double* vk = w.V + int64_t(k) * n;
@@ -360,7 +377,12 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       set_error("tnx_davidson1: non-finite Ritz value or residual");
       return TNX_ERR_INVALID_ARG;
     }
-    if (rnorm <= tol || k >= n) {
+    // primme's convention (linalg.py:86): residual relative to the operator scale, here |theta|
+    if (rnorm <= tol * fmax(1.0, fabs(theta)) || k >= n) {
+      converged = true;
+      break;
+    }
+    if (mixed && rnorm <= mixed_handover * fmax(1.0, fabs(theta))) {
       converged = true;
       break;
     }
@@ -403,8 +425,9 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       TNX_CUDA(cudaStreamSynchronize(st));
       theta = host[0];
       rnorm = sqrt(fmax(host[1], 0.0));
-      if (rnorm <= tol || ref >= max_refine || iters >= max_iter) break;
-      // GMRES(mg) on the projected shifted operator, x0 = 0, b = -r
+      if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta)) || ref >= max_refine || iters >= max_iter) break;
+      // right-preconditioned GMRES(mg) on P (H~ - theta) P M^-1, M = diag(H) - theta, x0 = 0,
+      // b = -r; the correction is delta = P M^-1 V y
       const double beta = rnorm;
       axpby_kernel<<<sblocks, DT, 0, st>>>(-1.0 / beta, w.t, 0.0, V, n);
       TNX_LAUNCH_CHECK();
@@ -415,9 +438,15 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       for (; j < mg && iters < max_iter; ++j) {
         double* vj = V + int64_t(j) * n;
         double* wj = Wv + int64_t(j) * n;
-        TNX_TRY(mixed_apply(W, vj, wj, chi_l, d, chi_r, dl, dr, w.mv, st));
+        // t = P M^-1 v_j
+        precond_kernel<<<sblocks, DT, 0, st>>>(vj, w.diag, theta, w.t, n);
+        TNX_LAUNCH_CHECK();
+        TNX_TRY(dots(w.x, n, 1, w.t, n, w.part, h, 1, nullptr, 0, st));
+        update_kernel<<<nch, DT, 0, st>>>(w.x, n, 1, h, w.t, n, w.part, nch);
+        TNX_LAUNCH_CHECK();
+        TNX_TRY(mixed_apply(W, w.t, wj, chi_l, d, chi_r, dl, dr, w.mv, st));
         ++iters;
-        axpby_kernel<<<sblocks, DT, 0, st>>>(-theta, vj, 1.0, wj, n);
+        axpby_kernel<<<sblocks, DT, 0, st>>>(-theta, w.t, 1.0, wj, n);
         TNX_LAUNCH_CHECK();
         // project out x
         TNX_TRY(dots(w.x, n, 1, wj, n, w.part, h, 1, nullptr, 0, st));
@@ -458,7 +487,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
         g[j + 1] = -sn[j] * g[j];
         g[j] = cs[j] * g[j];
         for (int i = 0; i <= j; ++i) Hh[i][j] = hcol[i];
-        if (fabs(g[j + 1]) <= 1e-3 * beta || hn == 0.0) {
+        if (fabs(g[j + 1]) <= 1e-2 * beta || hn == 0.0) {
           ++j;
           break;
         }
@@ -470,7 +499,12 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
         for (int q = i + 1; q < j; ++q) t -= Hh[i][q] * y.c[q];
         y.c[i] = Hh[i][i] != 0.0 ? t / Hh[i][i] : 0.0;
       }
-      combine_kernel<<<sblocks, DT, 0, st>>>(V, n, j, y, w.t, n);
+      combine_kernel<<<sblocks, DT, 0, st>>>(V, n, j, y, w.ax, n);
+      TNX_LAUNCH_CHECK();
+      precond_kernel<<<sblocks, DT, 0, st>>>(w.ax, w.diag, theta, w.t, n);
+      TNX_LAUNCH_CHECK();
+      TNX_TRY(dots(w.x, n, 1, w.t, n, w.part, h, 1, nullptr, 0, st));
+      update_kernel<<<nch, DT, 0, st>>>(w.x, n, 1, h, w.t, n, w.part, nch);
       TNX_LAUNCH_CHECK();
       axpby_kernel<<<sblocks, DT, 0, st>>>(1.0, w.t, 1.0, w.x, n);
       TNX_LAUNCH_CHECK();
@@ -478,7 +512,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       scale_kernel<<<sblocks, DT, 0, st>>>(w.x, n, nrm2);
       TNX_LAUNCH_CHECK();
     }
-    converged = rnorm <= tol;
+    converged = rnorm <= mixed_rtol * fmax(1.0, fabs(theta));
   }
   TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
   if (eval_out) *eval_out = theta;

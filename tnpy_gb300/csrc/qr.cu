@@ -193,9 +193,21 @@ __global__ void __cluster_dims__(QC, 1, 1) __launch_bounds__(QCT)
     }
     cluster.sync();
     const int owner = int(jrow / rpc);
-    double sigma = 0.0;
-    for (int qq = 0; qq < QC; ++qq) sigma += *cluster.map_shared_rank(&sig[par], qq);
-    const double alpha = *cluster.map_shared_rank(&alph[par], owner);
+    // one warp gathers the QC partial norms and alpha over DSMEM and publishes them locally
+    __shared__ double s_sigma, s_alpha;
+    if (warp == 0) {
+      double v = lane < QC ? *cluster.map_shared_rank(&sig[par], lane) : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) {
+        // fixed-order sum would differ from the tree sum across CTAs only if they used
+        // different orders; every CTA runs this same reduction, so results are identical
+        s_sigma = v;
+        s_alpha = *cluster.map_shared_rank(&alph[par], owner);
+      }
+    }
+    __syncthreads();
+    const double sigma = s_sigma;
+    const double alpha = s_alpha;
     double tj, beta, scale;
     if (sigma == 0.0) {
       tj = 0.0;
@@ -265,14 +277,19 @@ __global__ void __cluster_dims__(QC, 1, 1) __launch_bounds__(QCT)
     if (lane == 0) gram[a][b] = acc;
   }
   cluster.sync();
+  __shared__ double G[QB][QB + 1];
+  if (q == 0) {
+    // sum the partial Gram matrices of all CTAs, one (a, b) pair per thread
+    for (int pr = tid; pr < nb * nb; pr += QCT) {
+      const int a = pr / nb, b = pr % nb;
+      if (a >= b) continue;
+      double t = 0.0;
+      for (int qq = 0; qq < QC; ++qq) t += cluster.map_shared_rank(&gram[0][0], qq)[a * (QB + 1) + b];
+      G[a][b] = t;
+    }
+    __syncthreads();
+  }
   if (q == 0 && tid == 0) {
-    double G[QB][QB];
-    for (int a = 0; a < nb; ++a)
-      for (int b = a + 1; b < nb; ++b) {
-        double t = 0.0;
-        for (int qq = 0; qq < QC; ++qq) t += cluster.map_shared_rank(&gram[0][0], qq)[a * (QB + 1) + b];
-        G[a][b] = t;
-      }
     for (int b = 0; b < nb; ++b) {
       const double tb = s_tau[b];
       tau[b] = tb;

@@ -1,0 +1,72 @@
+"""Small fixed workloads for profiling single kernels (e.g. under ncu).
+
+    python -m tnpy_gb300.prof matvec --chi 1024      # split-BF16 tcgen05 matvec (+ FP64-class env)
+    python -m tnpy_gb300.prof env --chi 1024         # double-FP32 environment update
+    python -m tnpy_gb300.prof qr --m 2048 --n 1024   # Householder QR (cluster panel)
+    python -m tnpy_gb300.prof davidson --chi 512     # one mixed-precision local eigensolve
+
+Each mode runs two warm-up calls and then --reps calls of the same shapes, on random seeded
+inputs, and prints the CUDA-event time per call.
+"""
+from __future__ import annotations
+
+import argparse
+
+import torch
+
+from . import kernels as K
+
+
+def _time(fn, reps):
+    fn()
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("mode", choices=["matvec", "env", "qr", "davidson"])
+    p.add_argument("--chi", type=int, default=1024)
+    p.add_argument("--m", type=int, default=2048)
+    p.add_argument("--n", type=int, default=1024)
+    p.add_argument("--reps", type=int, default=3)
+    a = p.parse_args(argv)
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    rnd = lambda *shape: torch.randn(*shape, generator=g, dtype=torch.float64).to(dev)  # noqa: E731
+    chi = a.chi
+    if a.mode in ("matvec", "env", "davidson"):
+        L, R, W, x = rnd(chi, 5, chi), rnd(chi, 5, chi), rnd(5, 5, 2, 2), rnd(chi, 2, chi)
+        L = 0.5 * (L + L.permute(2, 1, 0))
+        R = 0.5 * (R + R.permute(2, 1, 0))
+        W = 0.5 * (W + W.permute(0, 1, 3, 2))
+        L, R, W = L.contiguous(), R.contiguous(), W.contiguous()
+    if a.mode == "matvec":
+        t = _time(lambda: K.matvec1(L, W, R, x, precision="mixed"), a.reps)
+        flops = 40 * chi**3 + 200 * chi**2
+        print(f"matvec mixed chi={chi}: {t:.3f} ms, {flops / t / 1e9:.1f} TFLOP/s algorithmic")
+    elif a.mode == "env":
+        t = _time(lambda: K.env_update(1, L, x, W, precision="df64"), a.reps)
+        print(f"env update df64 chi={chi}: {t:.3f} ms")
+    elif a.mode == "qr":
+        m = rnd(a.m, a.n)
+        t = _time(lambda: K.qr(m), a.reps)
+        print(f"qr {a.m}x{a.n}: {t:.3f} ms")
+    else:
+        def solve():
+            y = x.clone()
+            K.davidson1(L, W, R, y, tol=1e-8, precision="mixed")
+
+        t = _time(solve, a.reps)
+        print(f"davidson mixed chi={chi}: {t:.3f} ms")
+
+
+if __name__ == "__main__":
+    main()

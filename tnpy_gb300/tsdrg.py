@@ -185,6 +185,36 @@ def block_hamiltonians(pairs, dev) -> tuple[list[torch.Tensor], list[int]]:
     return mats, sizes
 
 
+KRON_MAX_NODE = 32
+KRON_MAX_P = 48
+
+
+def kron_eigh(pairs, chi: int, dev, precision: str = "mixed"):
+    """Lowest min(chi, m) eigenpairs of the two-block Hamiltonians of (W1, W2) pairs without
+    forming them (Kronecker-sum Chebyshev subspace iteration + FP64 Rayleigh-Ritz, one CTA per
+    block). Returns (evals [batch, keep] device, evecs [batch, max_m, keep] device, ks)."""
+    D = pairs[0][0].shape[1]
+    ms = [(w1.shape[2], w2.shape[2]) for w1, w2 in pairs]
+    ks = [min(chi, a * b) for a, b in ms]
+    ps = [min(a * b, k + max(8, k // 4), KRON_MAX_P) for (a, b), k in zip(ms, ks)]
+    keep = max(ks)
+    max_m = max(a * b for a, b in ms)
+    meta = torch.tensor([[a, b, w2.shape[1], k, p] for (a, b), k, p, (_, w2) in zip(ms, ks, ps, pairs)],
+                        dtype=torch.int32, device=dev).reshape(-1)
+    p1 = _ptr_array([w1 for w1, _ in pairs], dev)
+    p2 = _ptr_array([w2 for _, w2 in pairs], dev)
+    evals = torch.full((len(pairs), keep), float("nan"), dtype=torch.float64, device=dev)
+    evecs = torch.zeros((len(pairs), max_m, keep), dtype=torch.float64, device=dev)
+    code = K.precision_code(precision)
+    nbytes = lib.tnx_tsdrg_block_eigh_workspace_bytes(len(pairs), max_m, keep, code)
+    wp, wn = K.Workspace.get(nbytes, dev)
+    check("tnx_tsdrg_block_eigh", lib.tnx_tsdrg_block_eigh(ptr(p1), ptr(p2), ptr(meta), int(D), len(pairs), max_m,
+                                                         keep, code, ptr(evals), ptr(evecs), None, wp, wn,
+                                                         stream_ptr()))
+    del p1, p2, meta
+    return evals, evecs, ks
+
+
 def project(pairs_v, dev) -> list[torch.Tensor]:
     """Renormalised MPO tensors W' = V^T (W1 W2) V for (W1, W2, V) triples (tsdrg.py:633-669)."""
     if not pairs_v:
@@ -227,9 +257,10 @@ def project(pairs_v, dev) -> list[torch.Tensor]:
 class _Chain:
     """State of one realisation: coarse-grained MPO cache, horizon, gaps, kept vectors."""
 
-    def __init__(self, mpo: MatrixProductOperator, chi: int, dev):
+    def __init__(self, mpo: MatrixProductOperator, chi: int, dev, precision: str = "mixed"):
         self.n = mpo.n_sites
         self.chi = chi
+        self.precision = precision
         self.cache = [w.contiguous() for w in mpo.device_tensors(dev)]
         self.tree = TensorTree(self.n)
         self.gap: list[float] = []
@@ -246,18 +277,46 @@ def _gap(evals: np.ndarray, chi: int) -> float:
 
 
 def _solve(chains_bonds, dev):
-    """Solve the listed (chain, bond) blocks in one batched eigensolver call; returns per item
-    (host evals, device evecs [m, kept])."""
-    pairs = [(c.cache[b], c.cache[b + 1]) for c, b in chains_bonds]
-    mats, sizes = block_hamiltonians(pairs, dev)
-    chi = max(c.chi for c, _ in chains_bonds)
-    keep = min(chi, max(sizes))
-    evals, evecs = K.eigh_batched(mats, keep=keep)
-    ev_h = evals.cpu().numpy()
-    out = []
-    for i, ((c, _), m) in enumerate(zip(chains_bonds, sizes)):
-        kept = min(m, c.chi)
-        out.append((ev_h[i, :kept].copy(), evecs[i, :m, :kept].contiguous()))
+    """Solve the listed (chain, bond) blocks; returns per item (host evals, device evecs [m, kept]).
+
+    Blocks of at most 64 states (or with nodes beyond the Kronecker kernel's limits) are formed
+    densely and diagonalised by the batched Jacobi kernel; larger blocks go to the Kronecker
+    subspace eigensolver in the chain's precision. Each group is one launch."""
+    out = [None] * len(chains_bonds)
+    dense, kron = [], []
+    for i, (c, b) in enumerate(chains_bonds):
+        w1, w2 = c.cache[b], c.cache[b + 1]
+        m = w1.shape[2] * w2.shape[2]
+        if (m > 64 and w1.shape[2] <= KRON_MAX_NODE and w2.shape[2] <= KRON_MAX_NODE and c.chi <= 32
+                and w1.shape[1] <= 6):
+            kron.append(i)
+        else:
+            dense.append(i)
+    if dense:
+        pairs = [(chains_bonds[i][0].cache[chains_bonds[i][1]], chains_bonds[i][0].cache[chains_bonds[i][1] + 1])
+                 for i in dense]
+        mats, sizes = block_hamiltonians(pairs, dev)
+        chi = max(chains_bonds[i][0].chi for i in dense)
+        keep = min(chi, max(sizes))
+        evals, evecs = K.eigh_batched(mats, keep=keep)
+        ev_h = evals.cpu().numpy()
+        for j, (i, m) in enumerate(zip(dense, sizes)):
+            kept = min(m, chains_bonds[i][0].chi)
+            out[i] = (ev_h[j, :kept].copy(), evecs[j, :m, :kept].contiguous())
+    if kron:
+        groups: dict = {}
+        for i in kron:
+            groups.setdefault(chains_bonds[i][0].precision, []).append(i)
+        for prec, idx in groups.items():
+            pairs = [(chains_bonds[i][0].cache[chains_bonds[i][1]], chains_bonds[i][0].cache[chains_bonds[i][1] + 1])
+                     for i in idx]
+            chi = max(chains_bonds[i][0].chi for i in idx)
+            evals, evecs, ks = kron_eigh(pairs, chi, dev, precision=prec)
+            ev_h = evals.cpu().numpy()
+            for j, i in enumerate(idx):
+                m = pairs[j][0].shape[2] * pairs[j][1].shape[2]
+                kept = min(m, chains_bonds[i][0].chi)
+                out[i] = (ev_h[j, :kept].copy(), evecs[j, :m, :kept].contiguous())
     return out
 
 
@@ -309,12 +368,15 @@ def run_chains(chains: List[_Chain], dev):
 
 
 class TreeTensorNetworkSDRG:
-    def __init__(self, mpo: MatrixProductOperator, chi: int, device=None):
-        """tsdrg.py:500-528; all tensors live on ``device`` (default: current CUDA device)."""
+    def __init__(self, mpo: MatrixProductOperator, chi: int, device=None, precision: str = "mixed"):
+        """tsdrg.py:500-528; all tensors live on ``device`` (default: current CUDA device).
+
+        ``precision``: 'mixed' solves blocks above 64 states with the FP32 Kronecker subspace
+        iteration + FP64 Rayleigh-Ritz; 'fp64' runs that iteration in FP64."""
         self._mpo = mpo
         self._chi = int(chi)
         self._dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-        self._chain = _Chain(mpo, self._chi, self._dev)
+        self._chain = _Chain(mpo, self._chi, self._dev, precision)
 
     @property
     def mpo(self) -> MatrixProductOperator:
@@ -355,10 +417,10 @@ class BatchedTSDRG:
     every step is one launch of the block-Hamiltonian, eigensolver and projector kernels
     over all chains."""
 
-    def __init__(self, mpos: Sequence[MatrixProductOperator], chi: int, device=None):
+    def __init__(self, mpos: Sequence[MatrixProductOperator], chi: int, device=None, precision: str = "mixed"):
         self._dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.chi = int(chi)
-        self.chains = [_Chain(m, self.chi, self._dev) for m in mpos]
+        self.chains = [_Chain(m, self.chi, self._dev, precision) for m in mpos]
 
     def run(self):
         run_chains(self.chains, self._dev)
