@@ -3,15 +3,16 @@
 // (tnpy/linalg.py:64-87) called from FiniteDMRG.one_site_solver (tnpy/finite_dmrg.py:97-111).
 //
 // Basis V (orthonormal, FP64) and AV = H V live in the caller's workspace; each expansion
-//   1. orthogonalises the new direction against V twice (classical Gram-Schmidt, FP64),
-//   2. applies H (FP64 or split-BF16 tensor-core matvec),
+//   1. orthogonalises the new direction against V (classical Gram-Schmidt, FP64, with a
+//      second pass when the first removed more than half of its norm: DGKS),
+//   2. applies H (FP64, double-FP32 or split-BF16 tensor-core matvec),
 //   3. extends the projected matrix V^T H V (FP64 dots),
-//   4. solves it with the one-CTA Jacobi eigensolver (FP64 Rayleigh-Ritz),
+//   4. solves it for the lowest pair (Jacobi Rayleigh-Ritz, FP32 + FP64 correction),
 //   5. forms the Ritz vector, the residual r = H x - theta x and its norm, and the next
 //      direction t = r / (diag(H) - theta) (diagonal preconditioner).
-// The host loop reads two scalars per expansion to decide convergence. With the
-// split-BF16 matvec the final energy and residual are recomputed with one FP64 matvec
-// (defect correction), so the reported Rayleigh quotient is an FP64 one.
+// The host loop reads three scalars per expansion to decide convergence. With the
+// split-BF16 matvec a second, anchored phase takes the residual from the split-BF16
+// floor to FP64-class accuracy: one double-FP32 matvec per anchor (see davidson1).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -37,17 +38,31 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return t;  // valid in thread 0
 }
 
-// part[j*nchunk + chunk] = sum over the chunk of V[j][i] * w[i], j < k
+// part[j*nchunk + chunk] = sum over the chunk of V[j][i] * w[i], j < k. With a gate (|t|^2
+// before and after one Gram-Schmidt pass), the pass is skipped (zero partials) when the first
+// pass kept at least half of |t|^2: the DGKS criterion for a second classical Gram-Schmidt pass.
+__device__ __forceinline__ bool gs_pass_skipped(const double* gate) { return gate && gate[1] >= 0.5 * gate[0]; }
+
 __global__ void __launch_bounds__(DT) dots_kernel(const double* __restrict__ V, int64_t ldv,
                                                  const double* __restrict__ w, int64_t n,
-                                                 double* __restrict__ part, int nchunk) {
+                                                 double* __restrict__ part, int nchunk,
+                                                 const double* __restrict__ gate) {
   __shared__ double sh[DT / 32];
   const int j = blockIdx.y, chunk = blockIdx.x;
+  if (gs_pass_skipped(gate)) {
+    if (threadIdx.x == 0) part[j * nchunk + chunk] = 0.0;
+    return;
+  }
   const double* v = V + int64_t(j) * ldv;
-  double acc = 0.0;
-  for (int64_t i = int64_t(chunk) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT)
-    acc = fma(v[i], w[i], acc);
-  acc = block_sum(acc, sh);
+  double acc0 = 0.0, acc1 = 0.0;
+  const int64_t stride = int64_t(nchunk) * DT;
+  int64_t i = int64_t(chunk) * DT + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    acc0 = fma(v[i], w[i], acc0);
+    acc1 = fma(v[i + stride], w[i + stride], acc1);
+  }
+  if (i < n) acc0 = fma(v[i], w[i], acc0);
+  const double acc = block_sum(acc0 + acc1, sh);
   if (threadIdx.x == 0) part[j * nchunk + chunk] = acc;
 }
 
@@ -67,19 +82,32 @@ __global__ void __launch_bounds__(DT) reduce_kernel(const double* __restrict__ p
   }
 }
 
-// w -= sum_{j<k} h[j] V[j]; partial ||w||^2
+// w -= sum_{j<k} h[j] V[j]; partial ||w||^2 (a skipped gated pass only recomputes the norm)
 __global__ void __launch_bounds__(DT) update_kernel(const double* __restrict__ V, int64_t ldv, int k,
                                                    const double* __restrict__ h, double* __restrict__ w,
-                                                   int64_t n, double* __restrict__ part, int nchunk) {
+                                                   int64_t n, double* __restrict__ part, int nchunk,
+                                                   const double* __restrict__ gate) {
   __shared__ double sh[DT / 32];
   __shared__ double hs[MAXB];
+  const bool skip = gs_pass_skipped(gate);
   if (threadIdx.x < k) hs[threadIdx.x] = h[threadIdx.x];
   __syncthreads();
   double nrm = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
     double acc = w[i];
-    for (int j = 0; j < k; ++j) acc = fma(-hs[j], V[int64_t(j) * ldv + i], acc);
-    w[i] = acc;
+    if (!skip) {
+      int j = 0;
+      for (; j + 4 <= k; j += 4) {
+        const double v0 = V[int64_t(j) * ldv + i], v1 = V[int64_t(j + 1) * ldv + i];
+        const double v2 = V[int64_t(j + 2) * ldv + i], v3 = V[int64_t(j + 3) * ldv + i];
+        acc = fma(-hs[j], v0, acc);
+        acc = fma(-hs[j + 1], v1, acc);
+        acc = fma(-hs[j + 2], v2, acc);
+        acc = fma(-hs[j + 3], v3, acc);
+      }
+      for (; j < k; ++j) acc = fma(-hs[j], V[int64_t(j) * ldv + i], acc);
+      w[i] = acc;
+    }
     nrm = fma(acc, acc, nrm);
   }
   nrm = block_sum(nrm, sh);
@@ -109,11 +137,22 @@ __global__ void __launch_bounds__(DT) ritz_kernel(const double* __restrict__ V, 
   const double theta = theta_p[0];
   double nrm = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
-    double xv = 0.0, av = 0.0;
-    for (int j = 0; j < k; ++j) {
+    double xv = 0.0, av = 0.0, xw = 0.0, aw = 0.0;
+    int j = 0;
+    for (; j + 2 <= k; j += 2) {
+      const double v0 = V[int64_t(j) * ldv + i], v1 = V[int64_t(j + 1) * ldv + i];
+      const double a0 = AV[int64_t(j) * ldv + i], a1 = AV[int64_t(j + 1) * ldv + i];
+      xv = fma(ss[j], v0, xv);
+      av = fma(ss[j], a0, av);
+      xw = fma(ss[j + 1], v1, xw);
+      aw = fma(ss[j + 1], a1, aw);
+    }
+    if (j < k) {
       xv = fma(ss[j], V[int64_t(j) * ldv + i], xv);
       av = fma(ss[j], AV[int64_t(j) * ldv + i], av);
     }
+    xv += xw;
+    av += aw;
     const double r = av - theta * xv;
     x[i] = xv;
     ax[i] = av;
@@ -129,66 +168,6 @@ __global__ void __launch_bounds__(DT) ritz_kernel(const double* __restrict__ V, 
   }
   nrm = block_sum(nrm, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = nrm;
-}
-
-// r = ax - theta x with theta = (x . ax) given in th[0]; partial ||r||^2
-__global__ void __launch_bounds__(DT) resid_kernel(const double* __restrict__ x, const double* __restrict__ ax,
-                                                  const double* __restrict__ th, int64_t n,
-                                                  double* __restrict__ part, int nchunk) {
-  __shared__ double sh[DT / 32];
-  const double theta = th[0];
-  double nrm = 0.0;
-  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
-    const double r = ax[i] - theta * x[i];
-    nrm = fma(r, r, nrm);
-  }
-  nrm = block_sum(nrm, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = nrm;
-}
-
-// t = ax - theta x (theta = th[0]); partial ||t||^2
-__global__ void __launch_bounds__(DT) resid_write_kernel(const double* __restrict__ x, const double* __restrict__ ax,
-                                                        const double* __restrict__ th, double* __restrict__ t,
-                                                        int64_t n, double* __restrict__ part, int nchunk) {
-  __shared__ double sh[DT / 32];
-  const double theta = th[0];
-  double nrm = 0.0;
-  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
-    const double r = ax[i] - theta * x[i];
-    t[i] = r;
-    nrm = fma(r, r, nrm);
-  }
-  nrm = block_sum(nrm, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = nrm;
-}
-
-// out = in / (diag - theta), the diagonal preconditioner with its denominator kept >= 1e-2
-__global__ void precond_kernel(const double* __restrict__ in, const double* __restrict__ diag, double theta,
-                               double* __restrict__ out, int64_t n) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    double den = diag[i] - theta;
-    if (fabs(den) < 1e-2) den = den >= 0.0 ? 1e-2 : -1e-2;
-    out[i] = in[i] / den;
-  }
-}
-
-// y = a * x + b * y with host scalars
-__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* __restrict__ y, int64_t n) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-    y[i] = fma(a, x[i], b * y[i]);
-}
-
-// out = sum_{j<k} c[j] V[j]  (host coefficients passed by value in a small struct)
-struct Coef64 {
-  double c[64];
-};
-__global__ void combine_kernel(const double* __restrict__ V, int64_t ldv, int k, Coef64 c, double* __restrict__ out,
-                               int64_t n) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    double acc = 0.0;
-    for (int j = 0; j < k; ++j) acc = fma(c.c[j], V[int64_t(j) * ldv + i], acc);
-    out[i] = acc;
-  }
 }
 
 // after a restart to the single Ritz vector x: H = [[theta]], Ritz coefficients s = [1]
@@ -254,9 +233,9 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
 
 // h[0..k) = V[0..k) . w
 int dots(const double* V, int64_t ldv, int k, const double* w, int64_t n, double* part, double* out,
-         int out_stride, double* out2, int out2_stride, cudaStream_t st) {
+         int out_stride, double* out2, int out2_stride, cudaStream_t st, const double* gate = nullptr) {
   const int nch = nchunk_for(n);
-  dots_kernel<<<dim3(nch, k), DT, 0, st>>>(V, ldv, w, n, part, nch);
+  dots_kernel<<<dim3(nch, k), DT, 0, st>>>(V, ldv, w, n, part, nch, gate);
   TNX_LAUNCH_CHECK();
   reduce_kernel<<<k, DT, 0, st>>>(part, nch, out, out_stride, out2, out2_stride);
   TNX_LAUNCH_CHECK();
@@ -301,31 +280,50 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   if (int e = tnx_diag1(L, W, R, w.diag, chi_l, d, chi_r, dl, dr, st); e != TNX_OK) return e;
 
   int k = 0, iters = 0, precond = 1;
-  double theta = 0.0, rnorm = INFINITY;
-  bool converged = false;
-  // Stagnation: the split-BF16 operand is not exactly symmetric, so the residual of the
-  // mixed operator stops falling at ~1e-5 |H| (its rounding floor); the solve ends when the
-  // residual has not improved by 10% within `patience` matvecs (the FP64 defect correction
-  // below then gives the energy). The FP64 form uses a longer patience as a safeguard.
-  double best = INFINITY;
-  int best_it = 0;
-  const int patience = mixed ? 8 : 40;
-  const int max_refine = 6;  // defect-correction steps of the mixed form
-  // The mixed form hands over to the FP64-class defect correction once the split-BF16 residual
-  // is below 3e-6 |theta| or has stagnated at its ~1e-5 |H| floor (an earlier hand-over can leave
-  // the Davidson on an excited state that the correction then converges to), and refines the
-  // FP64-class residual
-  // to max(tol, 2e-7) |theta|: the energy error is quadratic in the residual,
-  // ~ (2e-7 |theta|)^2 / gap, i.e. below 1e-12 |E| for local gaps above 1e-2.
-  const double mixed_handover = 3e-6, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
-  for (;;) {
-    // -- new direction t -> V[k], orthogonalised against V[0..k) twice --
+  double theta = 0.0, rnorm = INFINITY, c0 = 1.0;
+
+  // Rayleigh-Ritz on V[0..k), Ritz vector x, AV-combination ax, residual norm and the next
+  // direction t; reads theta, ||r|| and the Ritz coefficient of V[0] back to the host.
+  auto rayleigh_ritz = [&]() -> int {
+    TNX_TRY(rr_lowest_f64(w.Hm, k, mb, w.evals, w.evecs, st));
+    ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, precond, w.x, w.ax, w.t, n,
+                                    w.part, nch);
+    TNX_LAUNCH_CHECK();
+    reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
+    TNX_LAUNCH_CHECK();
+    TNX_CUDA(cudaMemcpyAsync(host, w.evals, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaMemcpyAsync(host + 2, w.evecs, 8, cudaMemcpyDeviceToHost, st));
+    if (dflag) TNX_CUDA(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaStreamSynchronize(st));
+    if (hflag) {
+      set_error("tnx_davidson1: a bounded wait in the tensor-core matvec expired");
+      return TNX_ERR_TIMEOUT;
+    }
+    theta = host[0];
+    rnorm = sqrt(fmax(host[1], 0.0));
+    c0 = host[2];
+    if (!std::isfinite(theta) || !std::isfinite(rnorm)) {
+      set_error("tnx_davidson1: non-finite Ritz value or residual");
+      return TNX_ERR_INVALID_ARG;
+    }
+    return TNX_OK;
+  };
+
+  // One expansion: t -> V[k] (classical Gram-Schmidt, second pass by the DGKS criterion),
+  // AV[k] = H V[k], column k of V^T H V, Rayleigh-Ritz. With `anchored`, V[0] is a vector whose
+  // product AV[0] = H V[0] is FP64-class exact, and row 0 of the projected matrix is taken as
+  // AV[0] . V[k] (exact, H being symmetric) instead of V[0] . AV[k]. `*fell_in` reports a
+  // direction that vanished against the basis (nothing expanded).
+  auto expand = [&](bool anchored, bool* fell_in) -> int {
+    *fell_in = false;
     double* vk = w.V + int64_t(k) * n;
     TNX_CUDA(cudaMemcpyAsync(vk, w.t, n * 8, cudaMemcpyDeviceToDevice, st));
     TNX_TRY(dots(vk, n, 1, vk, n, w.part, nrm2, 1, nullptr, 0, st));
     for (int pass = 0; pass < 2 && k > 0; ++pass) {
-      TNX_TRY(dots(w.V, n, k, vk, n, w.part, h, 1, nullptr, 0, st));
-      update_kernel<<<nch, DT, 0, st>>>(w.V, n, k, h, vk, n, w.part, nch);
+      const double* gate = pass == 0 ? nullptr : nrm2;
+      TNX_TRY(dots(w.V, n, k, vk, n, w.part, h, 1, nullptr, 0, st, gate));
+      update_kernel<<<nch, DT, 0, st>>>(w.V, n, k, h, vk, n, w.part, nch, gate);
       TNX_LAUNCH_CHECK();
       reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, nrm2 + 1, 1, nullptr, 0);
       TNX_LAUNCH_CHECK();
@@ -338,44 +336,57 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
         set_error("tnx_davidson1: zero or non-finite start vector");
         return TNX_ERR_INVALID_ARG;
       }
+      *fell_in = true;
+      return TNX_OK;
+    }
+    scale_kernel<<<sblocks, DT, 0, st>>>(vk, n, nrm2 + 1);
+    TNX_LAUNCH_CHECK();
+    double* avk = w.AV + int64_t(k) * n;
+    TNX_TRY(matvec(vk, avk));
+    ++iters;
+    TNX_TRY(dots(w.V, n, k + 1, avk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
+    if (anchored && k > 0) TNX_TRY(dots(w.AV, n, 1, vk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
+    ++k;
+    return rayleigh_ritz();
+  };
+
+  // thick restart with the current Ritz vector
+  auto restart = [&]() -> int {
+    TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+    TNX_CUDA(cudaMemcpyAsync(w.AV, w.ax, n * 8, cudaMemcpyDeviceToDevice, st));
+    restart_kernel<<<1, 1, 0, st>>>(w.Hm, w.evals, w.evecs);
+    TNX_LAUNCH_CHECK();
+    k = 1;
+    return TNX_OK;
+  };
+
+  bool converged = false;
+  // Stagnation: the split-BF16 operand is not exactly symmetric, so the residual of the
+  // mixed operator stops falling at ~1e-5 |H| (its rounding floor); the first phase ends when
+  // the residual has not improved by 10% within `patience` matvecs. The FP64 form uses a longer
+  // patience as a safeguard.
+  double best = INFINITY;
+  int best_it = 0;
+  const int patience = mixed ? 8 : 40;
+  // The mixed form hands over to the anchored phase once the split-BF16 residual is below
+  // 3e-6 |theta| or has stagnated at its ~1e-5 |H| floor (an earlier hand-over can leave the
+  // solve on an excited state), and then converges the FP64-class residual to
+  // max(tol, 2e-7) |theta|: the energy error is quadratic in the residual,
+  // ~ (2e-7 |theta|)^2 / gap, i.e. below 1e-12 |E| for local gaps above 1e-2.
+  const double mixed_handover = 3e-6, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
+  for (;;) {
+    bool fell_in = false;
+    TNX_TRY(expand(false, &fell_in));
+    if (fell_in) {
       if (precond) {  // preconditioned direction fell inside the basis: retry with r
         precond = 0;
-        // recompute t = r from the current Ritz pair
         ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, 0, w.x, w.ax, w.t, n,
                                         w.part, nch);
         TNX_LAUNCH_CHECK();
         continue;
       }
-      break;  // stagnation: keep the current Ritz pair
-    }
-    scale_kernel<<<sblocks, DT, 0, st>>>(vk, n, nrm2 + 1);
-    TNX_LAUNCH_CHECK();
-    // -- AV[k] = H V[k]; projected matrix column k --
-    double* avk = w.AV + int64_t(k) * n;
-    TNX_TRY(matvec(vk, avk));
-    ++iters;
-    TNX_TRY(dots(w.V, n, k + 1, avk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
-    ++k;
-    // -- Rayleigh-Ritz (FP64 Jacobi on the k x k projected matrix, leading dim mb) --
-    TNX_TRY(rr_lowest_f64(w.Hm, k, mb, w.evals, w.evecs, st));
-    ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, precond, w.x, w.ax, w.t, n,
-                                    w.part, nch);
-    TNX_LAUNCH_CHECK();
-    reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
-    TNX_LAUNCH_CHECK();
-    TNX_CUDA(cudaMemcpyAsync(host, w.evals, 8, cudaMemcpyDeviceToHost, st));
-    TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
-    if (dflag) TNX_CUDA(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
-    TNX_CUDA(cudaStreamSynchronize(st));
-    if (hflag) {
-      set_error("tnx_davidson1: a bounded wait in the tensor-core matvec expired");
-      return TNX_ERR_TIMEOUT;
-    }
-    theta = host[0];
-    rnorm = sqrt(fmax(host[1], 0.0));
-    if (!std::isfinite(theta) || !std::isfinite(rnorm)) {
-      set_error("tnx_davidson1: non-finite Ritz value or residual");
-      return TNX_ERR_INVALID_ARG;
+      converged = mixed;  // the mixed form still refines below
+      break;
     }
     // primme's convention (linalg.py:86): residual relative to the operator scale, here |theta|
     if (rnorm <= tol * fmax(1.0, fabs(theta)) || k >= n) {
@@ -395,131 +406,72 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     }
     if (iters >= max_iter) break;
     precond = 1;
-    if (k == mb) {  // thick restart with the current Ritz vector
-      TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
-      TNX_CUDA(cudaMemcpyAsync(w.AV, w.ax, n * 8, cudaMemcpyDeviceToDevice, st));
-      restart_kernel<<<1, 1, 0, st>>>(w.Hm, w.evals, w.evecs);
-      TNX_LAUNCH_CHECK();
-      k = 1;
-    }
+    if (k == mb) TNX_TRY(restart());
   }
-  // -- output: unit Ritz vector; FP64-class Rayleigh quotient and residual for the mixed form --
   if (mixed) {
-    // Defect correction. The split-BF16 operand H~ only converges the Davidson to its own
-    // eigenvector; the FP64-class residual r = H x - theta x (double-FP32 matvec) then drives
-    // Jacobi-Davidson correction steps: solve (I - x x^T)(H~ - theta)(I - x x^T) delta = -r
-    // approximately with GMRES on the tensor-core matvec, x <- (x + delta) / ||x + delta||.
-    // Each step contracts the error by about (error of H~) * ||H|| / gap.
-    double* V = w.V;    // GMRES basis (the Davidson basis is no longer needed)
-    double* Wv = w.AV;  // operator output scratch
-    const int mg = mb - 1;
-    for (int ref = 0;; ++ref) {
-      TNX_TRY(matvec1_f64(L, W, R, w.x, w.ax, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true));
-      TNX_TRY(dots(w.x, n, 1, w.ax, n, w.part, h, 1, nullptr, 0, st));
-      resid_write_kernel<<<nch, DT, 0, st>>>(w.x, w.ax, h, w.t, n, w.part, nch);
-      TNX_LAUNCH_CHECK();
-      reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
-      TNX_LAUNCH_CHECK();
-      TNX_CUDA(cudaMemcpyAsync(host, h, 8, cudaMemcpyDeviceToHost, st));
-      TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
-      TNX_CUDA(cudaStreamSynchronize(st));
-      theta = host[0];
-      rnorm = sqrt(fmax(host[1], 0.0));
-      if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta)) || ref >= max_refine || iters >= max_iter) break;
-      // right-preconditioned GMRES(mg) on P (H~ - theta) P M^-1, M = diag(H) - theta, x0 = 0,
-      // b = -r; the correction is delta = P M^-1 V y
-      const double beta = rnorm;
-      axpby_kernel<<<sblocks, DT, 0, st>>>(-1.0 / beta, w.t, 0.0, V, n);
-      TNX_LAUNCH_CHECK();
-      double Hh[65][64] = {};
-      double cs[64], sn[64], g[65] = {};
-      g[0] = beta;
-      int j = 0;
-      for (; j < mg && iters < max_iter; ++j) {
-        double* vj = V + int64_t(j) * n;
-        double* wj = Wv + int64_t(j) * n;
-        // t = P M^-1 v_j
-        precond_kernel<<<sblocks, DT, 0, st>>>(vj, w.diag, theta, w.t, n);
-        TNX_LAUNCH_CHECK();
-        TNX_TRY(dots(w.x, n, 1, w.t, n, w.part, h, 1, nullptr, 0, st));
-        update_kernel<<<nch, DT, 0, st>>>(w.x, n, 1, h, w.t, n, w.part, nch);
-        TNX_LAUNCH_CHECK();
-        TNX_TRY(mixed_apply(W, w.t, wj, chi_l, d, chi_r, dl, dr, w.mv, st));
-        ++iters;
-        axpby_kernel<<<sblocks, DT, 0, st>>>(-theta, w.t, 1.0, wj, n);
-        TNX_LAUNCH_CHECK();
-        // project out x
-        TNX_TRY(dots(w.x, n, 1, wj, n, w.part, h, 1, nullptr, 0, st));
-        update_kernel<<<nch, DT, 0, st>>>(w.x, n, 1, h, wj, n, w.part, nch);
-        TNX_LAUNCH_CHECK();
-        // Arnoldi: two classical Gram-Schmidt passes against V[0..j]
-        double hcol[65] = {};
-        for (int pass = 0; pass < 2; ++pass) {
-          TNX_TRY(dots(V, n, j + 1, wj, n, w.part, h, 1, nullptr, 0, st));
-          update_kernel<<<nch, DT, 0, st>>>(V, n, j + 1, h, wj, n, w.part, nch);
-          TNX_LAUNCH_CHECK();
-          reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, nrm2, 1, nullptr, 0);
-          TNX_LAUNCH_CHECK();
-          double hh[64];
-          TNX_CUDA(cudaMemcpyAsync(hh, h, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, st));
-          TNX_CUDA(cudaMemcpyAsync(host, nrm2, 8, cudaMemcpyDeviceToHost, st));
-          TNX_CUDA(cudaStreamSynchronize(st));
-          for (int i = 0; i <= j; ++i) hcol[i] += hh[i];
-        }
-        const double hn = sqrt(fmax(host[0], 0.0));
-        hcol[j + 1] = hn;
-        if (hn > 0.0) {
-          double* vn = V + int64_t(j + 1) * n;
-          axpby_kernel<<<sblocks, DT, 0, st>>>(1.0 / hn, wj, 0.0, vn, n);
-          TNX_LAUNCH_CHECK();
-        }
-        // apply previous Givens rotations, then a new one zeroing hcol[j+1]
-        for (int i = 0; i < j; ++i) {
-          const double a = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
-          hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
-          hcol[i] = a;
-        }
-        const double den = sqrt(hcol[j] * hcol[j] + hcol[j + 1] * hcol[j + 1]);
-        cs[j] = den > 0.0 ? hcol[j] / den : 1.0;
-        sn[j] = den > 0.0 ? hcol[j + 1] / den : 0.0;
-        hcol[j] = den;
-        hcol[j + 1] = 0.0;
-        g[j + 1] = -sn[j] * g[j];
-        g[j] = cs[j] * g[j];
-        for (int i = 0; i <= j; ++i) Hh[i][j] = hcol[i];
-        if (fabs(g[j + 1]) <= 1e-2 * beta || hn == 0.0) {
-          ++j;
+    // Anchored phase. One double-FP32 matvec gives AV[0] = H x exactly for the current Ritz
+    // vector x = V[0]; the Davidson then continues with split-BF16 products for the new
+    // directions. Row 0 of the projected matrix (x^T H v = (H x)^T v) is exact, and the
+    // split-BF16 error E ~ 3e-5 |H| enters the Ritz value only through c^T E c and the
+    // residual through E c, where c (|c| = sqrt(1 - c0^2)) is the small part of the Ritz
+    // vector outside x. The residual of the anchored Ritz pair is therefore FP64-class
+    // while 3e-5 * 2|theta| * |c| stays below half the target; otherwise (or on stagnation)
+    // the phase re-anchors at the current Ritz vector with another double-FP32 matvec.
+    const int max_anchor = 6;
+    const double eps_h = 3e-5;  // bound on the split-BF16 matvec error relative to |H| ~ 2|theta|
+    converged = false;
+    for (int anchor = 0;; ++anchor) {
+      TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+      TNX_TRY(matvec1_f64(L, W, R, w.V, w.AV, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true));
+      TNX_TRY(dots(w.V, n, 1, w.AV, n, w.part, w.Hm, 1, nullptr, 0, st));
+      k = 1;
+      precond = 1;
+      TNX_TRY(rayleigh_ritz());
+      double drift = 0.0;  // sum of |c| over restarts inside this anchor
+      auto bound_ok = [&]() {
+        const double c = sqrt(fmax(1.0 - c0 * c0, 0.0));
+        return eps_h * 2.0 * fmax(1.0, fabs(theta)) * (drift + c) <= 0.5 * mixed_rtol * fmax(1.0, fabs(theta));
+      };
+      if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta))) {
+        converged = true;
+        break;
+      }
+      if (anchor >= max_anchor || iters >= max_iter) break;
+      best = rnorm;
+      best_it = iters;
+      bool reanchor = false;
+      while (!reanchor) {
+        bool fell_in = false;
+        TNX_TRY(expand(true, &fell_in));
+        if (fell_in) break;
+        if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta))) {
+          if (bound_ok()) converged = true;
           break;
         }
+        if (!bound_ok()) break;
+        if (rnorm < 0.9 * best) {
+          best = rnorm;
+          best_it = iters;
+        } else if (iters - best_it >= patience) {
+          break;
+        }
+        if (iters >= max_iter) break;
+        if (k == mb) {
+          drift += sqrt(fmax(1.0 - c0 * c0, 0.0));
+          TNX_TRY(restart());
+        }
       }
-      // y = R^-1 g (upper triangular), delta = V y, x <- (x + delta) / ||x + delta||
-      Coef64 y = {};
-      for (int i = j - 1; i >= 0; --i) {
-        double t = g[i];
-        for (int q = i + 1; q < j; ++q) t -= Hh[i][q] * y.c[q];
-        y.c[i] = Hh[i][i] != 0.0 ? t / Hh[i][i] : 0.0;
-      }
-      combine_kernel<<<sblocks, DT, 0, st>>>(V, n, j, y, w.ax, n);
-      TNX_LAUNCH_CHECK();
-      precond_kernel<<<sblocks, DT, 0, st>>>(w.ax, w.diag, theta, w.t, n);
-      TNX_LAUNCH_CHECK();
-      TNX_TRY(dots(w.x, n, 1, w.t, n, w.part, h, 1, nullptr, 0, st));
-      update_kernel<<<nch, DT, 0, st>>>(w.x, n, 1, h, w.t, n, w.part, nch);
-      TNX_LAUNCH_CHECK();
-      axpby_kernel<<<sblocks, DT, 0, st>>>(1.0, w.t, 1.0, w.x, n);
-      TNX_LAUNCH_CHECK();
-      TNX_TRY(dots(w.x, n, 1, w.x, n, w.part, nrm2, 1, nullptr, 0, st));
-      scale_kernel<<<sblocks, DT, 0, st>>>(w.x, n, nrm2);
-      TNX_LAUNCH_CHECK();
+      if (converged || iters >= max_iter) break;
     }
-    converged = rnorm <= mixed_rtol * fmax(1.0, fabs(theta));
   }
+  // the Ritz vector of the last Rayleigh-Ritz step, unit norm
   TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
   if (eval_out) *eval_out = theta;
   if (resid_out) *resid_out = rnorm;
   if (iters_out) *iters_out = iters;
   if (!converged) {
-    set_error("tnx_davidson1: %d matvecs, residual %.3e > tol %.3e", iters, rnorm, tol);
+    set_error("tnx_davidson1: %d matvecs, residual %.3e > tol %.3e", iters, rnorm,
+              mixed ? mixed_rtol * fmax(1.0, fabs(theta)) : tol);
     return TNX_ERR_NOT_CONVERGED;
   }
   return TNX_OK;

@@ -221,20 +221,32 @@ namespace {
 
 constexpr int RW_MAX = 64;
 
-__global__ void __launch_bounds__(32) rr_lowest_warp_kernel(const double* __restrict__ A, int n, int ld,
-                                                          double* __restrict__ eval, double* __restrict__ evec) {
+constexpr int RR_T = 128;  // threads of the Rayleigh-Ritz kernel
+
+// Lowest eigenpair of a small symmetric matrix (n <= 64): parallel-ordered cyclic Jacobi in
+// FP32 (the rotation angles of one round by one thread per pair, the row and column updates
+// spread over all threads), then three FP64 correction steps of the lowest Ritz vector against
+// the FP32 eigenbasis, s <- s - sum_j v_j (v_j . r) / (l_j - theta), and the FP64 Rayleigh
+// quotient. FP32 rounding keeps regenerating off-diagonal entries at ~6e-8 |A|_F, so the sweeps
+// stop once every off-diagonal entry is below 1e-6 |A|_F; the FP64 steps take it from there.
+__global__ void __launch_bounds__(RR_T) rr_lowest_warp_kernel(const double* __restrict__ A, int n, int ld,
+                                                            double* __restrict__ eval, double* __restrict__ evec) {
   extern __shared__ double sm_d[];
   double* Ad = sm_d;                                      // n x n FP64
   float* Af = reinterpret_cast<float*>(Ad + n * n);       // n x (n+1) FP32
   float* Vf = Af + n * (n + 1);                           // n x (n+1) FP32
   double* s = reinterpret_cast<double*>(Vf + n * (n + 1) + ((n * (n + 1)) & 1));  // n FP64 (8-byte aligned)
-  double* r = s + n;
+  double* r = s + n;                                      // n
+  double* f = r + n;                                      // n correction coefficients
   __shared__ float cs[32], ss[32];
   __shared__ int pp[32], qq[32];
-  const int lane = threadIdx.x;
+  __shared__ float red[RR_T / 32];
+  __shared__ double redd[RR_T / 32];
+  __shared__ int s_any, s_imin;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nf = n + 1;
   float fro = 0.f;
-  for (int e = lane; e < n * n; e += 32) {
+  for (int e = tid; e < n * n; e += RR_T) {
     const int i = e / n, j = e % n;
     const double v = A[int64_t(i) * ld + j];
     Ad[e] = v;
@@ -243,112 +255,140 @@ __global__ void __launch_bounds__(32) rr_lowest_warp_kernel(const double* __rest
     fro += float(v) * float(v);
   }
   for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+  if (lane == 0) red[warp] = fro;
+  __syncthreads();
+  fro = 0.f;
+  for (int w = 0; w < RR_T / 32; ++w) fro += red[w];
   fro = sqrtf(fro);
-  __syncwarp();
+  const float thresh = 1e-6f * fro;
   if (n > 1) {
     const int np = n + (n & 1), npairs = np / 2;
+    if (tid == 0) s_any = 0;
+    __syncthreads();
     for (int sweep = 0; sweep < 30; ++sweep) {
-      int any = 0;
       for (int rnd = 0; rnd < np - 1; ++rnd) {
-        if (lane < npairs) {
-          int p = lane == 0 ? 0 : 1 + (lane - 1 + rnd) % (np - 1);
-          int q = 1 + (np - 1 - lane - 1 + rnd) % (np - 1);
+        if (tid < npairs) {
+          int p = tid == 0 ? 0 : 1 + (tid - 1 + rnd) % (np - 1);
+          int q = 1 + (np - 1 - tid - 1 + rnd) % (np - 1);
           if (p > q) { int t = p; p = q; q = t; }
           float c = 1.f, sn = 0.f;
           if (q < n) {
             const float apq = Af[p * nf + q], app = Af[p * nf + p], aqq = Af[q * nf + q];
-            if (fabsf(apq) > 1e-7f * fro && fabsf(apq) > 1e-7f * sqrtf(fabsf(app * aqq))) {
+            if (fabsf(apq) > thresh) {
               const float th = (aqq - app) / (2.f * apq);
               const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(1.f + th * th));
               c = 1.f / sqrtf(1.f + t * t);
               sn = t * c;
-              any = 1;
+              s_any = 1;
             }
           }
-          pp[lane] = p; qq[lane] = q; cs[lane] = c; ss[lane] = sn;
+          pp[tid] = p; qq[tid] = q; cs[tid] = c; ss[tid] = sn;
         }
-        __syncwarp();
-        if (lane < npairs && ss[lane] != 0.f) {
-          const int p = pp[lane], q = qq[lane];
-          const float c = cs[lane], sn = ss[lane];
-          for (int i = 0; i < n; ++i) {  // columns p, q
-            const float a = Af[i * nf + p], b = Af[i * nf + q];
-            Af[i * nf + p] = c * a - sn * b;
-            Af[i * nf + q] = sn * a + c * b;
-          }
+        __syncthreads();
+        // A <- A J: columns p, q (pairs touch disjoint columns)
+        for (int e = tid; e < npairs * n; e += RR_T) {
+          const int k = e / n, i = e % n;
+          const float sn = ss[k];
+          if (sn == 0.f) continue;
+          const int p = pp[k], q = qq[k];
+          const float c = cs[k];
+          const float a = Af[i * nf + p], b = Af[i * nf + q];
+          Af[i * nf + p] = c * a - sn * b;
+          Af[i * nf + q] = sn * a + c * b;
         }
-        __syncwarp();
-        if (lane < npairs && ss[lane] != 0.f) {
-          const int p = pp[lane], q = qq[lane];
-          const float c = cs[lane], sn = ss[lane];
-          for (int j = 0; j < n; ++j) {  // rows p, q; V columns p, q
-            const float a = Af[p * nf + j], b = Af[q * nf + j];
-            Af[p * nf + j] = c * a - sn * b;
-            Af[q * nf + j] = sn * a + c * b;
-            const float va = Vf[j * nf + p], vb = Vf[j * nf + q];
-            Vf[j * nf + p] = c * va - sn * vb;
-            Vf[j * nf + q] = sn * va + c * vb;
-          }
-          Af[p * nf + q] = 0.f;
-          Af[q * nf + p] = 0.f;
+        __syncthreads();
+        // A <- J^T A: rows p, q (disjoint rows); V <- V J
+        for (int e = tid; e < npairs * n; e += RR_T) {
+          const int k = e / n, j = e % n;
+          const float sn = ss[k];
+          if (sn == 0.f) continue;
+          const int p = pp[k], q = qq[k];
+          const float c = cs[k];
+          const float a = Af[p * nf + j], b = Af[q * nf + j];
+          Af[p * nf + j] = c * a - sn * b;
+          Af[q * nf + j] = sn * a + c * b;
+          const float va = Vf[j * nf + p], vb = Vf[j * nf + q];
+          Vf[j * nf + p] = c * va - sn * vb;
+          Vf[j * nf + q] = sn * va + c * vb;
         }
-        __syncwarp();
+        __syncthreads();
+        if (tid < npairs && ss[tid] != 0.f) {
+          Af[pp[tid] * nf + qq[tid]] = 0.f;
+          Af[qq[tid] * nf + pp[tid]] = 0.f;
+        }
+        __syncthreads();
       }
-      any = __any_sync(0xffffffffu, any);
+      // every thread reads the flag before thread 0 clears it for the next sweep
+      const int any = s_any;
+      __syncthreads();
       if (!any) break;
+      if (tid == 0) s_any = 0;
+      __syncthreads();
     }
   }
   // lowest FP32 eigenvalue
-  int imin = 0;
-  float dmin = Af[0];
-  for (int i = 1; i < n; ++i)
-    if (Af[i * nf + i] < dmin) { dmin = Af[i * nf + i]; imin = i; }
-  for (int i = lane; i < n; i += 32) s[i] = double(Vf[i * nf + imin]);
-  __syncwarp();
+  if (tid == 0) {
+    int imin = 0;
+    float dmin = Af[0];
+    for (int i = 1; i < n; ++i)
+      if (Af[i * nf + i] < dmin) { dmin = Af[i * nf + i]; imin = i; }
+    s_imin = imin;
+  }
+  __syncthreads();
+  const int imin = s_imin;
+  for (int i = tid; i < n; i += RR_T) s[i] = double(Vf[i * nf + imin]);
+  __syncthreads();
+  const double floor = 1e-6 * (double(fro) + 1e-300);
   double theta = 0.0;
   for (int step = 0; step < 4; ++step) {
-    // normalise s, r = A s, theta = s.r, r -= theta s
+    // normalise s (n <= 64 entries: summed by every warp redundantly), r = A s, theta = s . r
     double nn = 0.0;
     for (int i = lane; i < n; i += 32) nn += s[i] * s[i];
     for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    __syncthreads();
     const double inv = 1.0 / sqrt(nn);
-    for (int i = lane; i < n; i += 32) s[i] *= inv;
-    __syncwarp();
+    for (int i = tid; i < n; i += RR_T) s[i] *= inv;
+    __syncthreads();
     double th = 0.0;
-    for (int i = lane; i < n; i += 32) {
+    for (int i = tid; i < n; i += RR_T) {
       double acc = 0.0;
       for (int j = 0; j < n; ++j) acc = fma(Ad[i * n + j], s[j], acc);
       r[i] = acc;
       th = fma(acc, s[i], th);
     }
     for (int o = 16; o > 0; o >>= 1) th += __shfl_xor_sync(0xffffffffu, th, o);
+    if (lane == 0) redd[warp] = th;
+    __syncthreads();
+    th = 0.0;
+    for (int w = 0; w < RR_T / 32; ++w) th += redd[w];
     theta = th;
-    __syncwarp();
     if (step == 3) break;
-    for (int i = lane; i < n; i += 32) r[i] -= theta * s[i];
-    __syncwarp();
-    // s -= sum_{j != imin} v_j (v_j . r) / (lambda_j - theta)
-    for (int j = 0; j < n; ++j) {
-      if (j == imin) continue;
+    for (int i = tid; i < n; i += RR_T) r[i] -= theta * s[i];
+    __syncthreads();
+    // f_j = (v_j . r) / (l_j - theta), one warp per j; (near-)degenerate partners keep f_j = 0
+    for (int j = warp; j < n; j += RR_T / 32) {
       double dot = 0.0;
       for (int i = lane; i < n; i += 32) dot = fma(double(Vf[i * nf + j]), r[i], dot);
       for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-      double den = double(Af[j * nf + j]) - theta;
-      const double floor = 1e-6 * (double(fro) + 1e-300);
-      if (fabs(den) < floor) continue;  // (near-)degenerate partner: stays in the eigenspace
-      const double f = dot / den;
-      for (int i = lane; i < n; i += 32) s[i] -= f * double(Vf[i * nf + j]);
+      const double den = double(Af[j * nf + j]) - theta;
+      if (lane == 0) f[j] = (j != imin && fabs(den) >= floor) ? dot / den : 0.0;
     }
-    __syncwarp();
+    __syncthreads();
+    for (int i = tid; i < n; i += RR_T) {
+      double acc = s[i];
+      for (int j = 0; j < n; ++j) acc = fma(-f[j], double(Vf[i * nf + j]), acc);
+      s[i] = acc;
+    }
+    __syncthreads();
   }
-  if (lane == 0) eval[0] = theta;
-  for (int i = lane; i < n; i += 32) evec[i] = s[i];
+  if (tid == 0) eval[0] = theta;
+  for (int i = tid; i < n; i += RR_T) evec[i] = s[i];
 }
 
 }  // namespace
 
 size_t rr_lowest_smem(int n) {
-  return size_t(n) * n * 8 + 2 * size_t(n) * (n + 1) * 4 + 8 + 2 * size_t(n) * 8;
+  return size_t(n) * n * 8 + 2 * size_t(n) * (n + 1) * 4 + 8 + 3 * size_t(n) * 8;
 }
 
 int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cudaStream_t st) {
@@ -363,7 +403,7 @@ int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cu
     attr = true;
   }
   profile_mark(KF_EIGH, st, true);
-  rr_lowest_warp_kernel<<<1, 32, rr_lowest_smem(n), st>>>(A, n, ld, eval, evec);
+  rr_lowest_warp_kernel<<<1, RR_T, rr_lowest_smem(n), st>>>(A, n, ld, eval, evec);
   profile_mark(KF_EIGH, st, false);
   TNX_LAUNCH_CHECK();
   return TNX_OK;

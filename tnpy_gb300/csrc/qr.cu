@@ -7,12 +7,16 @@
 // differ from the SVD's U and S V^T by an orthogonal change of gauge on the bond, which
 // leaves energies, environments (up to that gauge) and the next local problem unchanged.
 //
-// Blocked right-looking Householder on a column-major copy: each 32-column panel is
-// factored by one CTA (reflectors + the compact-WY T factor), the trailing matrix is
-// updated with three FP64 GEMMs (W = V^T C, W = T^T W, C -= V W), and Q is formed by
-// applying the panels backwards to [I; 0].
+// Blocked right-looking Householder on a column-major copy: each 64- (or 32-) column panel
+// is factored by one thread-block cluster holding the panel in shared memory (reflectors +
+// the compact-WY T factor; one-CTA kernel for panels too tall for a cluster), the trailing
+// matrix is updated with three FP64-class GEMMs (W = V^T C, W = T^T W, C -= V W), and Q is
+// formed by applying the panels backwards to [I; 0].
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <mutex>
 
 #include "tnx_internal.cuh"
 
@@ -21,11 +25,8 @@ namespace cg = cooperative_groups;
 namespace tnx {
 namespace {
 
-constexpr int QB = 32;        // panel width
+constexpr int QB = 32;        // panel width of the one-CTA panel kernel
 constexpr int QT = 512;       // threads of the panel kernel
-constexpr int QC = 8;         // CTAs of the cluster panel kernel
-constexpr int QCT = 256;      // threads per CTA of the cluster panel kernel
-constexpr int QC_ROWS = 512;  // panel rows held per CTA (shared memory)
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -143,174 +144,229 @@ __global__ void __launch_bounds__(QT) panel_kernel(double* __restrict__ F, int64
   }
 }
 
-// Cluster form of panel_kernel: the panel's rows are split over QC CTAs of one thread-block
-// cluster, each holding its rows in shared memory. Per column, the partial norms and the
-// partial dot products of the reflector with the remaining columns are exchanged through
-// distributed shared memory with two cluster barriers, so the FP64 work of a panel is
-// spread over QC SMs instead of one. Every CTA combines the partials in the same order, so
-// all CTAs compute bitwise-identical reflector coefficients.
-__global__ void __cluster_dims__(QC, 1, 1) __launch_bounds__(QCT)
-    panel_cluster_kernel(double* __restrict__ F, int64_t m, int64_t j0, int nb, double* __restrict__ tau,
-                         double* __restrict__ T) {
+// Cluster form of the panel factorisation: the panel's rows are split over CL CTAs of one
+// thread-block cluster, each holding its rows in shared memory. Column jj costs ONE cluster
+// barrier: before it, every CTA publishes in its exchange slot the partial dot products of
+// column jj (below its pivot) with every column c >= jj (c = jj gives the norm), the pivot
+// row jj (its owner only) and the partial dot products v_a . v_{jj-1} that extend the
+// compact-WY T factor by one column (LAPACK dlarft recurrence, forward/columnwise). After the
+// barrier each CTA sums the CL partials in rank order, so all CTAs derive bitwise-identical
+// beta, tau and v^T x_c = x_c[jj] + scale * sum_{i>jj} x_jj[i] x_c[i] without a second
+// exchange, update their rows, and compute the next column's partials in the same pass.
+// Slots are double-buffered, so the barrier of step jj also orders the reads of step jj-1.
+//
+// Each step: one thread derives the column's scalars; phase A forms v = scale * x_jj and the
+// updated column jj+1 once per row (FP64 arithmetic is scarce on this part); phase B (before
+// the barrier arrives) updates columns c > jj+1 and forms the partial dots; phase C (between
+// arrive and wait) stores v and column jj+1 and extends T on rank 0.
+constexpr int PT = 256;  // threads per CTA of the cluster panel kernel
+
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory");
+}
+
+template <int NB, int CL>
+__global__ void __launch_bounds__(PT) panel_cl_kernel(double* __restrict__ F, int64_t m, int64_t j0, int nb,
+                                                      int ld, double* __restrict__ tau_out,
+                                                      double* __restrict__ T_out) {
+  constexpr int TPC = PT / NB;  // threads per panel column, interleaved over rows
   cg::cluster_group cluster = cg::this_cluster();
   const int q = int(cluster.block_rank());
-  extern __shared__ double pl[];  // [QB][QC_ROWS] column-major panel rows of this CTA
-  __shared__ double sig[2], alph[2], dots[2][QB];
-  __shared__ double gram[QB][QB + 1];
-  __shared__ double s_tau[QB];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int NW = QCT / 32;
+  extern __shared__ double pl[];  // [NB][ld] column-major panel rows of this CTA, then vr[ld], vnr[ld]
+  double* vr = pl + NB * ld;      // reflector of the current column over this CTA's rows
+  double* vnr = vr + ld;          // next column after the current reflector
+  __shared__ double slot[2][3 * NB];  // s[NB] partial dots, piv[NB] pivot row, z[NB] T dots
+  __shared__ double S[NB], P[NB], Z[NB], taus[NB], sc[4];
+  __shared__ double Ts[NB][NB + 1];  // T factor, rank 0 only, row a held by thread a
+  const int tid = threadIdx.x, ci = tid / TPC, h = tid % TPC;
   const int64_t mp = m - j0;
-  const int64_t rpc = (mp + QC - 1) / QC;
-  const int64_t r0 = int64_t(q) * rpc;                          // first panel row of this CTA
+  const int64_t rpc = (mp + CL - 1) / CL;
+  const int64_t r0 = int64_t(q) * rpc;  // first panel row of this CTA
   const int rows = int(r0 >= mp ? 0 : (mp - r0 < rpc ? mp - r0 : rpc));
-  for (int e = tid; e < nb * rows; e += QCT) {
+  for (int e = tid; e < nb * rows; e += PT) {
     const int c = e / rows, r = e % rows;
-    pl[c * QC_ROWS + r] = F[(j0 + c) * m + j0 + r0 + r];
+    pl[c * ld + r] = F[(j0 + c) * m + j0 + r0 + r];
   }
   __syncthreads();
+  // partials of pivot 0: s[c] = sum_{row > 0} x_0 x_c, pivot row 0 from rank 0
+  {
+    double acc = 0.0;
+    if (ci < nb) {
+      const double* xc = pl + ci * ld;
+      const int rs = r0 > 0 ? 0 : 1;
+      for (int i = rs / TPC; i * TPC < rows; ++i) {
+        const int r = i * TPC + h;
+        if (r >= rs && r < rows) acc = fma(pl[r], xc[r], acc);
+      }
+    }
+#pragma unroll
+    for (int o = TPC / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (ci < nb && h == 0) {
+      slot[0][ci] = acc;
+      if (r0 == 0 && rows > 0) slot[0][NB + ci] = pl[ci * ld];
+    }
+  }
+  cluster_arrive_release();
+  cluster_wait_acquire();
   for (int jj = 0; jj < nb; ++jj) {
     const int par = jj & 1;
-    const int64_t jrow = jj;  // pivot row in panel coordinates
-    // -- partial sigma over rows > pivot; the owner of the pivot row publishes alpha
-    double part = 0.0;
-    for (int r = tid; r < rows; r += QCT) {
-      const int64_t gr = r0 + r;
-      if (gr > jrow) {
-        const double x = pl[jj * QC_ROWS + r];
-        part = fma(x, x, part);
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    __shared__ double red[NW];
-    if (lane == 0) red[warp] = part;
-    __syncthreads();
-    if (tid == 0) {
-      double t = 0.0;
-      for (int w = 0; w < NW; ++w) t += red[w];
-      sig[par] = t;
-      if (jrow >= r0 && jrow < r0 + rows) alph[par] = pl[jj * QC_ROWS + (jrow - r0)];
-    }
-    cluster.sync();
-    const int owner = int(jrow / rpc);
-    // one warp gathers the QC partial norms and alpha over DSMEM and publishes them locally
-    __shared__ double s_sigma, s_alpha;
-    if (warp == 0) {
-      double v = lane < QC ? *cluster.map_shared_rank(&sig[par], lane) : 0.0;
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) {
-        // fixed-order sum would differ from the tree sum across CTAs only if they used
-        // different orders; every CTA runs this same reduction, so results are identical
-        s_sigma = v;
-        s_alpha = *cluster.map_shared_rank(&alph[par], owner);
-      }
-    }
-    __syncthreads();
-    const double sigma = s_sigma;
-    const double alpha = s_alpha;
-    double tj, beta, scale;
-    if (sigma == 0.0) {
-      tj = 0.0;
-      beta = alpha;
-      scale = 0.0;
-    } else {
-      const double nrm = sqrt(alpha * alpha + sigma);
-      beta = alpha >= 0.0 ? -nrm : nrm;
-      tj = (beta - alpha) / beta;
-      scale = 1.0 / (alpha - beta);
-    }
-    // -- reflector v in place (v_pivot = 1 implicit; the pivot slot keeps beta = R_jj)
-    if (tj != 0.0)
-      for (int r = tid; r < rows; r += QCT)
-        if (r0 + r > jrow) pl[jj * QC_ROWS + r] *= scale;
-    if (tid == 0) {
-      s_tau[jj] = tj;
-      if (jrow >= r0 && jrow < r0 + rows) pl[jj * QC_ROWS + (jrow - r0)] = beta;
-    }
-    __syncthreads();
-    // -- partial dots of v with the remaining columns (warp per column, lanes over rows)
-    const int rem = nb - jj - 1;
-    for (int c = warp; c < rem; c += NW) {
-      double acc = 0.0;
-      if (tj != 0.0)
-        for (int r = lane; r < rows; r += 32) {
-          const int64_t gr = r0 + r;
-          if (gr < jrow) continue;
-          const double vi = gr == jrow ? 1.0 : pl[jj * QC_ROWS + r];
-          acc = fma(vi, pl[(jj + 1 + c) * QC_ROWS + r], acc);
-        }
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) dots[par][c] = acc;
-    }
-    cluster.sync();
-    if (tj != 0.0 && rem > 0) {
-      __shared__ double wv[QB];
-      if (tid < rem) {
+    const int owner = int(jj / rpc);
+    if (tid < NB) {
+      const int c = tid;
+      if (c >= jj && c < nb) {
         double t = 0.0;
-        for (int qq = 0; qq < QC; ++qq) t += *cluster.map_shared_rank(&dots[par][tid], qq);
-        wv[tid] = tj * t;
+#pragma unroll
+        for (int qq = 0; qq < CL; ++qq) t += cluster.map_shared_rank(&slot[par][0], qq)[c];
+        S[c] = t;
+        P[c] = cluster.map_shared_rank(&slot[par][NB], owner)[c];
       }
-      __syncthreads();
-      for (int e = tid; e < rem * rows; e += QCT) {
-        const int c = e / rows, r = e % rows;
-        const int64_t gr = r0 + r;
-        if (gr < jrow) continue;
-        const double vi = gr == jrow ? 1.0 : pl[jj * QC_ROWS + r];
-        pl[(jj + 1 + c) * QC_ROWS + r] -= wv[c] * vi;
+    } else if (tid < 2 * NB && q == 0) {
+      const int a = tid - NB;
+      if (a < jj - 1) {
+        double t = 0.0;
+#pragma unroll
+        for (int qq = 0; qq < CL; ++qq) t += cluster.map_shared_rank(&slot[par][2 * NB], qq)[a];
+        Z[a] = t;
       }
     }
     __syncthreads();
-  }
-  // -- partial Gram of the reflectors, G[a][b] = v_a . v_b (a < b), reduced on rank 0
-  for (int pr = warp; pr < nb * nb; pr += NW) {
-    const int a = pr / nb, b = pr % nb;
-    if (a >= b) continue;
+    // column scalars once (FP64 sqrt and divisions are slow on this part's FP64 pipe)
+    if (tid == 0) {
+      const double sigma = S[jj], alpha = P[jj];
+      double tj = 0.0, beta = alpha, scale = 0.0;
+      if (sigma != 0.0) {
+        const double nrm = sqrt(alpha * alpha + sigma);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tj = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      sc[0] = tj;
+      sc[1] = beta;
+      sc[2] = scale;
+      sc[3] = jj + 1 < nb ? tj * (P[jj + 1] + scale * S[jj + 1]) : 0.0;  // w of column jj+1
+      taus[jj] = tj;
+    }
+    __syncthreads();
+    const double tj = sc[0], beta = sc[1], scale = sc[2], wn = sc[3];
+    const bool has_next = jj + 1 < nb;
+    double* nxt = slot[par ^ 1];
+    double* xj = pl + jj * ld;
+    double* xn = pl + (jj + 1) * ld;
+    const int64_t lj = jj - r0;  // local row of pivot jj (outside [0, rows) if another CTA holds it)
+    // ---- phase A: v_jj = scale * x_jj below the pivot (1 at it) and the updated column jj+1,
+    // once per row
+    for (int r = int(lj > 0 ? lj : 0) + tid; r < rows; r += PT) {
+      const double v = r == lj ? 1.0 : scale * xj[r];
+      vr[r] = v;
+      if (has_next) vnr[r] = xn[r] - wn * v;
+    }
+    __syncthreads();
+    // ---- phase B: update columns c > jj+1, partial dots of column jj+1 with c >= jj+1 below
+    // pivot jj+1 (norm at c = jj+1), pivot row jj+1, T dots v_c . v_jj for c < jj
     double acc = 0.0;
-    for (int r = lane; r < rows; r += 32) {
-      const int64_t gr = r0 + r;
-      if (gr < b) continue;
-      const double va = pl[a * QC_ROWS + r];  // gr >= b > a: stored part of v_a
-      const double vb = gr == b ? 1.0 : pl[b * QC_ROWS + r];
-      acc = fma(va, vb, acc);
-    }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) gram[a][b] = acc;
-  }
-  cluster.sync();
-  __shared__ double G[QB][QB + 1];
-  if (q == 0) {
-    // sum the partial Gram matrices of all CTAs, one (a, b) pair per thread
-    for (int pr = tid; pr < nb * nb; pr += QCT) {
-      const int a = pr / nb, b = pr % nb;
-      if (a >= b) continue;
-      double t = 0.0;
-      for (int qq = 0; qq < QC; ++qq) t += cluster.map_shared_rank(&gram[0][0], qq)[a * (QB + 1) + b];
-      G[a][b] = t;
-    }
-    __syncthreads();
-  }
-  if (q == 0 && tid == 0) {
-    for (int b = 0; b < nb; ++b) {
-      const double tb = s_tau[b];
-      tau[b] = tb;
-      for (int a = 0; a < b; ++a) {
-        double t = 0.0;
-        for (int c = a; c < b; ++c) t += T[c * QB + a] * G[c][b];
-        T[b * QB + a] = -tb * t;
+    if (ci < nb && ci != jj) {
+      double* xc = pl + ci * ld;
+      const int64_t ln = lj + 1;
+      const bool own_ln = ln >= 0 && ln < rows && ln % TPC == h;
+      if (ci == jj + 1) {
+        if (own_ln) nxt[NB + ci] = vnr[ln];
+        const int rs = int(lj + 2 > 0 ? lj + 2 : 0);
+        for (int i = rs / TPC; i * TPC < rows; ++i) {
+          const int r = i * TPC + h;
+          if (r >= rs && r < rows) acc = fma(vnr[r], vnr[r], acc);
+        }
+      } else if (ci > jj) {
+        const double wc = tj * (P[ci] + scale * S[ci]);
+        if (lj >= 0 && lj < rows && lj % TPC == h) xc[lj] -= wc;  // v_jj[jj] = 1
+        if (own_ln) {
+          const double val = xc[ln] - wc * vr[ln];
+          xc[ln] = val;
+          nxt[NB + ci] = val;  // pivot row of step jj+1
+        }
+        const int rs = int(lj + 2 > 0 ? lj + 2 : 0);
+        for (int i = rs / TPC; i * TPC < rows; ++i) {
+          const int r = i * TPC + h;
+          if (r < rs || r >= rows) continue;
+          const double val = xc[r] - wc * vr[r];
+          xc[r] = val;
+          acc = fma(vnr[r], val, acc);
+        }
+      } else {
+        const int rs = int(lj > 0 ? lj : 0);
+        for (int i = rs / TPC; i * TPC < rows; ++i) {
+          const int r = i * TPC + h;
+          if (r >= rs && r < rows) acc = fma(xc[r], vr[r], acc);
+        }
       }
-      T[b * QB + b] = tb;
-      for (int a = b + 1; a < QB; ++a) T[b * QB + a] = 0.0;
     }
-    for (int b = nb; b < QB; ++b)
-      for (int a = 0; a < QB; ++a) T[b * QB + a] = 0.0;
+#pragma unroll
+    for (int o = TPC / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (ci < nb && ci != jj && h == 0) {
+      if (ci > jj) nxt[ci] = acc;
+      else nxt[2 * NB + ci] = acc;
+    }
+    cluster_arrive_release();
+    __syncthreads();
+    // ---- phase C: store v_jj and beta, the updated column jj+1, extend T by column jj-1
+    {
+      for (int r = int(lj > 0 ? lj : 0) + tid; r < rows; r += PT) {
+        xj[r] = r == lj ? beta : vr[r];
+        if (has_next) xn[r] = vnr[r];
+      }
+      if (q == 0 && jj >= 1 && tid < jj) {
+        const int k = jj - 1, a = tid;
+        if (a == k) {
+          Ts[k][k] = taus[k];
+        } else {
+          double t = 0.0;
+          for (int c = a; c < k; ++c) t = fma(Ts[a][c], Z[c], t);
+          Ts[a][k] = -taus[k] * t;
+        }
+      }
+    }
+    // the next gather rewrites S, P and Z, which phase C of other threads still reads
+    __syncthreads();
+    cluster_wait_acquire();
   }
-  // write the factored rows back; the last barrier keeps every CTA's shared memory alive
-  // until rank 0 has read the Gram partials
-  for (int e = tid; e < nb * rows; e += QCT) {
+  // last T column from the final exchange
+  if (q == 0 && tid >= NB && tid < 2 * NB) {
+    const int a = tid - NB;
+    if (a < nb - 1) {
+      double t = 0.0;
+#pragma unroll
+      for (int qq = 0; qq < CL; ++qq) t += cluster.map_shared_rank(&slot[nb & 1][2 * NB], qq)[a];
+      Z[a] = t;
+    }
+  }
+  __syncthreads();
+  if (q == 0 && tid < nb) {
+    const int k = nb - 1, a = tid;
+    if (a == k) {
+      Ts[k][k] = taus[k];
+    } else {
+      double t = 0.0;
+      for (int c = a; c < k; ++c) t = fma(Ts[a][c], Z[c], t);
+      Ts[a][k] = -taus[k] * t;
+    }
+  }
+  __syncthreads();
+  if (q == 0) {
+    for (int e = tid; e < NB * NB; e += PT) {
+      const int b = e / NB, a = e % NB;  // T_out column-major, ld NB
+      T_out[e] = (a <= b && b < nb) ? Ts[a][b] : 0.0;
+    }
+    for (int b = tid; b < NB; b += PT) tau_out[b] = b < nb ? taus[b] : 0.0;
+  }
+  for (int e = tid; e < nb * rows; e += PT) {
     const int c = e / rows, r = e % rows;
-    F[(j0 + c) * m + j0 + r0 + r] = pl[c * QC_ROWS + r];
+    F[(j0 + c) * m + j0 + r0 + r] = pl[c * ld + r];
   }
-  cluster.sync();
+  // no CTA leaves while rank 0 may still read its slots
+  cluster_arrive_release();
+  cluster_wait_acquire();
 }
 
 // dst (row-major rows x cols) <-> col-major transposed copy
@@ -371,19 +427,21 @@ unsigned blocks_for(int64_t total) {
 struct QrWs {
   double *F, *Qc, *tau, *T, *Vp, *W1, *W2, *part;
 };
+constexpr int QBMAX = 64;  // widest panel
 constexpr int QR_SPLIT_MAX = 16;
 inline int qr_nsplit(int64_t k) {
   int64_t s = (k + 255) / 256;
   return int(s < 1 ? 1 : (s > QR_SPLIT_MAX ? QR_SPLIT_MAX : s));
 }
 
+// sized for QBMAX-wide panels, which also covers QB-wide ones
 size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off += align_up(bytes); return o; };
-  const int64_t np = (n + QB - 1) / QB;
-  size_t oF = take(m * n * 8), oQ = take(m * n * 8), otau = take(np * QB * 8), oT = take(np * QB * QB * 8),
-         oV = take(m * QB * 8), oW1 = take(n * QB * 8), oW2 = take(n * QB * 8),
-         oP = take(size_t(QR_SPLIT_MAX) * n * QB * 8);
+  const int64_t np = (n + QBMAX - 1) / QBMAX;
+  size_t oF = take(m * n * 8), oQ = take(m * n * 8), otau = take(np * QBMAX * 8),
+         oT = take(np * QBMAX * QBMAX * 8), oV = take(m * QBMAX * 8), oW1 = take(n * QBMAX * 8),
+         oW2 = take(n * QBMAX * 8), oP = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8);
   if (w && base) {
     char* b = static_cast<char*>(base);
     w->F = reinterpret_cast<double*>(b + oF);
@@ -398,30 +456,136 @@ size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
   return off;
 }
 
+// Leading dimension of a CTA's panel rows: a multiple of 16 doubles plus the threads per column,
+// so the TPC row-interleaved threads of 16 / TPC neighbouring columns hit distinct banks.
+inline int panel_ld(int64_t rpc, int tpc) { return int((rpc + 15) / 16 * 16 + tpc); }
+
+// One-time attribute setup of a cluster panel instantiation: largest dynamic shared memory it
+// may use and whether a cluster of CL CTAs with that much shared memory can be scheduled.
+struct PanelKernelInfo {
+  bool ok = false;
+  size_t max_dyn = 0;
+};
+
+template <int NB, int CL>
+const PanelKernelInfo& panel_info() {
+  static PanelKernelInfo info;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    auto k = panel_cl_kernel<NB, CL>;
+    cudaFuncAttributes fa{};
+    int dev = 0, optin = 0;
+    if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    const size_t dyn = size_t(optin) > fa.sharedSizeBytes ? size_t(optin) - fa.sharedSizeBytes : 0;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)) != cudaSuccess ||
+        (CL > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
+      cudaGetLastError();
+      return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CL;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(PT);
+    cfg.dynamicSmemBytes = dyn;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      clusters = 0;
+    }
+    info.max_dyn = dyn;
+    info.ok = clusters > 0;
+  });
+  return info;
+}
+
+template <int NB, int CL>
+int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* T, cudaStream_t st) {
+  const int64_t rpc = (m - j0 + CL - 1) / CL;
+  const int ld = panel_ld(rpc, PT / NB);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(CL);
+  cfg.blockDim = dim3(PT);
+  cfg.dynamicSmemBytes = size_t(NB + 2) * ld * sizeof(double);
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  TNX_CUDA(cudaLaunchKernelEx(&cfg, panel_cl_kernel<NB, CL>, F, m, j0, nb, ld, tau, T));
+  TNX_LAUNCH_CHECK();
+  return TNX_OK;
+}
+
+// Panel plan of one QR: width nb (64 or 32) and cluster size cl (16 or 8; 0 = one-CTA panel,
+// for panels too tall for a cluster's shared memory). Wider panels give the trailing-update
+// GEMMs a longer K; 16-CTA clusters (where the device schedules them) spread the panel's FP64
+// arithmetic over twice the SMs of the portable 8.
+// TNX_QR_CLUSTER=8 or 16 restricts the cluster size (tuning).
+struct PanelPlan {
+  int nb, cl;
+};
+
+template <int NB, int CL>
+bool panel_fits(int64_t m) {
+  const PanelKernelInfo& info = panel_info<NB, CL>();
+  const int64_t rpc = (m + CL - 1) / CL;
+  return info.ok && size_t(NB + 2) * panel_ld(rpc, PT / NB) * sizeof(double) <= info.max_dyn;
+}
+
+PanelPlan plan_panels(int64_t m) {
+  static const int only = [] {
+    const char* e = getenv("TNX_QR_CLUSTER");
+    return e ? atoi(e) : 0;
+  }();
+  const bool c8 = only == 0 || only == 8, c16 = only == 0 || only == 16;
+  if (c16 && panel_fits<64, 16>(m)) return {64, 16};
+  if (c8 && panel_fits<64, 8>(m)) return {64, 8};
+  if (c16 && panel_fits<32, 16>(m)) return {32, 16};
+  if (c8 && panel_fits<32, 8>(m)) return {32, 8};
+  return {QB, 0};
+}
+
+int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, double* tau, double* T,
+                 cudaStream_t st) {
+  profile_mark(KF_QR_PANEL, st, true);
+  int rc = TNX_OK;
+  if (pp.nb == 64 && pp.cl == 8) rc = launch_panel<64, 8>(F, m, j0, nb, tau, T, st);
+  else if (pp.nb == 64 && pp.cl == 16) rc = launch_panel<64, 16>(F, m, j0, nb, tau, T, st);
+  else if (pp.nb == 32 && pp.cl == 8) rc = launch_panel<32, 8>(F, m, j0, nb, tau, T, st);
+  else if (pp.nb == 32 && pp.cl == 16) rc = launch_panel<32, 16>(F, m, j0, nb, tau, T, st);
+  else {
+    panel_kernel<<<1, QT, 0, st>>>(F, m, j0, nb, tau, T);
+    TNX_LAUNCH_CHECK();
+  }
+  profile_mark(KF_QR_PANEL, st, false);
+  return rc;
+}
+
 }  // namespace
 
 // Factor the column-major m x n matrix in w.F (m >= n) and form Q (column-major) in w.Qc.
 int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false) {
-  const int64_t np = (n + QB - 1) / QB;
+  const PanelPlan pp = plan_panels(m);
+  const int NB = pp.nb;
+  const int64_t np = (n + NB - 1) / NB;
   for (int64_t p = 0; p < np; ++p) {
-    const int64_t j0 = p * QB;
-    const int nb = int(n - j0 < QB ? n - j0 : QB);
-    if (m - j0 <= int64_t(QC) * QC_ROWS) {
-      static bool attr = false;
-      const size_t smem = size_t(QB) * QC_ROWS * sizeof(double);
-      if (!attr) {
-        TNX_CUDA(cudaFuncSetAttribute(panel_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        attr = true;
-      }
-      profile_mark(KF_QR_PANEL, st, true);
-      panel_cluster_kernel<<<QC, QCT, smem, st>>>(w.F, m, j0, nb, w.tau + p * QB, w.T + p * QB * QB);
-      profile_mark(KF_QR_PANEL, st, false);
-    } else {
-      profile_mark(KF_QR_PANEL, st, true);
-      panel_kernel<<<1, QT, 0, st>>>(w.F, m, j0, nb, w.tau + p * QB, w.T + p * QB * QB);
-      profile_mark(KF_QR_PANEL, st, false);
-    }
-    TNX_LAUNCH_CHECK();
+    const int64_t j0 = p * NB;
+    const int nb = int(n - j0 < NB ? n - j0 : NB);
+    double* Tp = w.T + p * NB * NB;  // column-major nb x nb, ld NB
+    TNX_TRY(factor_panel(pp, w.F, m, j0, nb, w.tau + p * NB, Tp, st));
     const int64_t mp = m - j0, nc = n - j0 - nb;
     if (nc > 0) {
       panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, w.Vp);
@@ -430,9 +594,8 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
       // W1^T (nc x nb) = C^T V  (thin output, long K: split over K)
       TNX_TRY(gemm_f64_splitk(false, true, nc, nb, mp, 1.0, C, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
                               st, df));
-      // W2^T = W1^T T   (T column-major nb x nb with ld QB == row-major T^T)
-      TNX_TRY(gemm_fp64_class(df, false, true, nc, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2,
-                              nb, 0, 1, st));
+      // W2^T = W1^T T   (T column-major with ld NB == row-major T^T)
+      TNX_TRY(gemm_fp64_class(df, false, true, nc, nb, nb, 1.0, w.W1, nb, 0, Tp, NB, 0, 0.0, w.W2, nb, 0, 1, st));
       // C^T -= W2^T V^T
       TNX_TRY(gemm_fp64_class(df, false, false, nc, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, C, m, 0, 1, st));
     }
@@ -441,18 +604,18 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
   eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.Qc, m, n);
   TNX_LAUNCH_CHECK();
   for (int64_t p = np - 1; p >= 0; --p) {
-    const int64_t j0 = p * QB;
-    const int nb = int(n - j0 < QB ? n - j0 : QB);
+    const int64_t j0 = p * NB;
+    const int nb = int(n - j0 < NB ? n - j0 : NB);
     const int64_t mp = m - j0, nq = n - j0;
+    const double* Tp = w.T + p * NB * NB;
     panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, w.Vp);
     TNX_LAUNCH_CHECK();
     double* Qs = w.Qc + j0 * m + j0;  // column-major mp x nq, ld m
     // W1^T (nq x nb) = Qs^T V
     TNX_TRY(gemm_f64_splitk(false, true, nq, nb, mp, 1.0, Qs, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
                             st, df));
-    // W2^T = W1^T T^T  -> B = T^T: op(B)[k][n] = T[n][k] = Tcm[k*QB + n] -> row-major, ld QB
-    TNX_TRY(gemm_fp64_class(df, false, false, nq, nb, nb, 1.0, w.W1, nb, 0, w.T + p * QB * QB, QB, 0, 0.0, w.W2,
-                            nb, 0, 1, st));
+    // W2^T = W1^T T^T  -> B = T^T: op(B)[k][n] = T[n][k] = Tcm[k*NB + n] -> row-major, ld NB
+    TNX_TRY(gemm_fp64_class(df, false, false, nq, nb, nb, 1.0, w.W1, nb, 0, Tp, NB, 0, 0.0, w.W2, nb, 0, 1, st));
     // Qs^T -= W2^T V^T
     TNX_TRY(gemm_fp64_class(df, false, false, nq, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, Qs, m, 0, 1, st));
   }

@@ -2,19 +2,41 @@
 
     python -m tnpy_gb300.prof matvec --chi 1024      # split-BF16 tcgen05 matvec (+ FP64-class env)
     python -m tnpy_gb300.prof env --chi 1024         # double-FP32 environment update
-    python -m tnpy_gb300.prof qr --m 2048 --n 1024   # Householder QR (cluster panel)
+    python -m tnpy_gb300.prof qr --m 2048 --n 1024   # Householder QR (cluster panel), FP64 GEMMs
+    python -m tnpy_gb300.prof gauge --chi 1024       # one-site gauge move (QR with double-FP32 GEMMs)
     python -m tnpy_gb300.prof davidson --chi 512     # one mixed-precision local eigensolve
 
 Each mode runs two warm-up calls and then --reps calls of the same shapes, on random seeded
-inputs, and prints the CUDA-event time per call.
+inputs, and prints the CUDA-event time per call and its split over the library's kernel
+families (tnx_profile_begin / tnx_profile_end).
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 
 import torch
 
 from . import kernels as K
+from ._lib import lib
+
+FAMILIES = ["tcgen05 GEMM", "FP64-class GEMM", "vector", "QR panel", "eigh", "other"]
+
+
+def _families(fn, reps):
+    """Per-family device time of `reps` calls (ms per call), from the library's event profiler."""
+    out = {}
+    for fam, name in enumerate(FAMILIES):
+        torch.cuda.synchronize()
+        lib.tnx_profile_begin(fam)
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        n, ms, fl, by = ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        lib.tnx_profile_end(ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(by))
+        if n.value:
+            out[name] = (n.value / reps, ms.value / reps)
+    return out
 
 
 def _time(fn, reps):
@@ -30,9 +52,13 @@ def _time(fn, reps):
     return s.elapsed_time(e) / reps
 
 
+def _fmt(fam):
+    return ", ".join(f"{k}: {n:.0f} launches {ms:.2f} ms" for k, (n, ms) in fam.items())
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("mode", choices=["matvec", "env", "qr", "davidson"])
+    p.add_argument("mode", choices=["matvec", "env", "qr", "gauge", "davidson"])
     p.add_argument("--chi", type=int, default=1024)
     p.add_argument("--m", type=int, default=2048)
     p.add_argument("--n", type=int, default=1024)
@@ -57,15 +83,28 @@ def main(argv=None):
         print(f"env update df64 chi={chi}: {t:.3f} ms")
     elif a.mode == "qr":
         m = rnd(a.m, a.n)
-        t = _time(lambda: K.qr(m), a.reps)
-        print(f"qr {a.m}x{a.n}: {t:.3f} ms")
+        fn = lambda: K.qr(m)  # noqa: E731
+        t = _time(fn, a.reps)
+        print(f"qr {a.m}x{a.n}: {t:.3f} ms  " + _fmt(_families(fn, a.reps)))
+    elif a.mode == "gauge":
+        site, nb = rnd(chi, 2, chi), rnd(chi, 2, chi)
+
+        def fn():
+            K.gauge_move(1, site.clone(), nb.clone(), precision="mixed")
+
+        t = _time(fn, a.reps)
+        print(f"gauge move df64 chi={chi}: {t:.3f} ms  " + _fmt(_families(fn, a.reps)))
     else:
+        stats = {}
+
         def solve():
             y = x.clone()
-            K.davidson1(L, W, R, y, tol=1e-8, precision="mixed")
+            stats["out"] = K.davidson1(L, W, R, y, tol=1e-8, precision="mixed")
 
         t = _time(solve, a.reps)
-        print(f"davidson mixed chi={chi}: {t:.3f} ms")
+        e, rn, its, ok = stats["out"]
+        print(f"davidson mixed chi={chi}: {t:.3f} ms, {its} matvecs, residual {rn:.2e}, converged {ok}  "
+              + _fmt(_families(solve, a.reps)))
 
 
 if __name__ == "__main__":
