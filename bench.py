@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--tol", type=float, default=1e-8)
     p.add_argument("--seed", type=int, default=1234)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the matvec-form and tSDRG measurements")
+    p.add_argument("--tsdrg-realizations", type=int, default=64)
     return p.parse_args()
 
 
@@ -144,6 +146,79 @@ def cpu_sample(a, matvecs_per_site: float | None = None):
                       f"split + env, {n - 1} site updates per sweep (full-chi site cost for every site)",
             "seconds_per_site": per_site, "matvecs_per_site": mv,
             "matvec_tflops": (40 * cl * cr * max(cl, cr) + 200 * cl * cr) / t_mv / 1e12}
+
+
+# ------------------------------------------------------------------ secondary measurements
+def matvec_forms(f, site: int):
+    """Matvec TFLOP/s of the three arithmetic forms on the bench chain's own local operator at
+    ``site`` (algorithmic flops 4 chi_l chi_r max(chi) D d + 2 chi_l chi_r D^2 d^2 per product),
+    and the lowest local eigenvalue from the mixed and the FP64 Davidson on that operator."""
+    import torch
+
+    from tnpy_gb300 import kernels as K
+
+    L, W, R = f.env.site_operator(site)
+    x = f.mps.tensors[site].contiguous()
+    cl, d, cr = x.shape
+    D = W.shape[0]
+    flops = 4.0 * cl * cr * max(cl, cr) * D * d + 2.0 * cl * cr * D * D * d * d
+    out = {"site": site, "shape": [cl, d, cr], "flops_per_matvec": flops}
+    for form, reps in (("mixed", 10), ("df64", 3), ("fp64", 2)):
+        K.matvec1(L, W, R, x, precision=form)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            K.matvec1(L, W, R, x, precision=form)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[form] = {"ms": ms, "tflops": flops / (ms / 1e3) / 1e12}
+    evs = {}
+    for form in ("mixed", "fp64"):
+        y = x.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e, rn, its, ok = K.davidson1(L, W, R, y, tol=1e-10, precision=form, max_iter=400)
+        torch.cuda.synchronize()
+        evs[form] = {"eval": e, "residual": rn, "matvecs": its, "converged": bool(ok),
+                     "s": time.perf_counter() - t0}
+    out["local_eigensolve"] = evs
+    out["local_dE_rel_mixed_vs_fp64"] = abs(evs["mixed"]["eval"] - evs["fp64"]["eval"]) / abs(evs["fp64"]["eval"])
+    return out
+
+
+def tsdrg_rate(n_real: int, with_cpu: bool):
+    """Batched tSDRG on `n_real` random-coupling chains J_i = (1-u_i)^(1/delta), u = RandomState(10000+r),
+    n=128, chi=32, delta=1, h=0 (realisations/s), with one realisation of the CPU restatement timed
+    on the host cores beside it."""
+    import torch
+
+    import tnpy_gb300 as tg
+
+    n, chi = 128, 32
+    mpos = [tg.model.RandomCouplingHeisenberg(n, delta=1.0, seed=10000 + r).mpo for r in range(n_real)]
+    tg.BatchedTSDRG(mpos[:2], chi=chi).run()  # warm-up (kernels, workspaces)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = tg.BatchedTSDRG(mpos, chi=chi).run()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out = {"workload": f"tsdrg_random_coupling_n{n}_chi{chi}_delta1_h0", "realizations": n_real,
+           "value": n_real / dt, "unit": "realizations/s", "seconds": dt, "e0_realization0": float(b.evals[0][0]),
+           "note": "h=0 is SU(2) symmetric: chi=32 cuts through degenerate multiplets, so the kept states "
+                   "(and the variational energy) depend on rounding in any implementation"}
+    if with_cpu:
+        from oracle import models as om
+        from oracle import tsdrg as ots
+
+        m = tg.model.RandomCouplingHeisenberg(n, delta=1.0, seed=10000)
+        t0 = time.perf_counter()
+        ots.TreeTensorNetworkSDRG(om.random_coupling_heisenberg_mpo(n, m.couplings, 0.0), chi).run()
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / tc, "unit": "realizations/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "one realisation (r=0) of the numpy restatement"}
+    return out
 
 
 # ------------------------------------------------------------------ reference arm
@@ -275,6 +350,9 @@ def run_ours(a):
     line["davidson_matvecs_per_site"] = mv_per_site
     if rank == 0 and world == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_sample(a, mv_per_site)
+    if rank == 0 and not a.no_extras:
+        line["matvec_forms"] = matvec_forms(f, a.n // 2)
+        line["tsdrg"] = tsdrg_rate(a.tsdrg_realizations, with_cpu=(world == 1 and not a.no_cpu))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

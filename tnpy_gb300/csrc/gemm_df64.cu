@@ -1,14 +1,15 @@
 // Double-FP32 ("df64") GEMM: FP64 in, FP64 out, arithmetic on the FP32 pipe.
 //
 // GB300 issues FP64 at ~2 FMA/clock/SM but FP32 at 128 FMA/clock/SM. Each FP64 operand is
-// split into a float pair (hi = fl32(x), lo = fl32(x - hi)); a product is formed as
+// split into a float pair (hi, lo) by integer operations (split_df); a product is formed as
 //   p = hi_a*hi_b, e = fma(hi_a, hi_b, -p) + hi_a*lo_b + lo_a*hi_b   (error-free + cross terms)
 // and accumulated with an error-free two-sum into a (hi, lo) float pair. About 11 FP32
 // operations per product give ~2^-48 relative accuracy per product, i.e. FP64-class
 // environments, residuals and gauge moves at several times the native FP64 rate.
 //
 // Tiling: 64 x 128 output tile per CTA, 16-deep K slab, 256 threads, 4 x 8 outputs per
-// thread at stride 16 (conflict-free shared-memory reads), operands staged as float pairs.
+// thread at stride 16 (conflict-free shared-memory reads), operands staged as float pairs;
+// the next slab's global loads are issued into registers before the current slab's products.
 #include <cuda_runtime.h>
 
 #include "tnx_internal.cuh"
@@ -29,6 +30,41 @@ __device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, f
   const float err = (ch - (s - bv)) + (p - bv);
   ch = s;
   cl += err + e;
+}
+
+// x = hi + lo with |x - hi - lo| < 2^-47 |x| for 2^-100 < |x| < FLT_MAX: hi is x truncated to
+// 24 significant bits, lo the remaining 29 mantissa bits truncated to 24 (a float denormal
+// when it falls below 2^-126). Integer operations only: the split takes no FP64-pipe issue
+// slots (float(x - double(float(x))) costs a DADD and two conversions on that pipe). Zero and
+// |x| < 2^-126 give (+-0, +-0); |x| > FLT_MAX gives (+-inf, 0), NaN gives (NaN, 0).
+__device__ __forceinline__ void split_df(double x, float& hi, float& lo) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned hw = unsigned(u >> 32), lw = unsigned(u);
+  const unsigned sign = hw & 0x80000000u;
+  const int e = int((hw >> 20) & 0x7ffu);
+  const int fe = e - 896;  // float exponent field: e - 1023 + 127
+  const unsigned m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
+  const unsigned r29 = lw & 0x1fffffffu;
+  if (fe <= 0) {
+    hi = __uint_as_float(sign);
+    lo = hi;
+    return;
+  }
+  if (fe >= 255) {
+    hi = __uint_as_float(sign | 0x7f800000u | ((e == 2047 && (m23 | r29)) ? 0x400000u : 0u));
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | (unsigned(fe) << 23) | m23);
+  unsigned lb = sign;
+  if (r29 != 0u) {
+    const int p = 31 - __clz(r29);  // leading one of the remainder
+    const unsigned full = p >= 23 ? (r29 >> (p - 23)) : (r29 << (23 - p));
+    const int le = e - 948 + p;  // float exponent field of lo: (e - 1075 + p) + 127
+    if (le > 0) lb |= (unsigned(le) << 23) | (full & 0x7fffffu);
+    else if (1 - le < 24) lb |= full >> (1 - le);
+  }
+  lo = __uint_as_float(lb);
 }
 
 template <bool TA, bool TB>
@@ -55,44 +91,47 @@ __global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int
 #pragma unroll
     for (int j = 0; j < RJ; ++j) ch[i][j] = cl[i][j] = 0.f;
 
-  for (int64_t k0 = 0; k0 < K; k0 += DK) {
+  constexpr int LA = (DM * DK) / DT, LB = (DN * DK) / DT;  // slab elements per thread
+  double pa[LA], pb[LB];
+  // global -> registers for the slab at k0 (zero outside the matrix)
+  auto fetch = [&](int64_t k0) {
 #pragma unroll
-    for (int r = 0; r < (DM * DK) / DT; ++r) {
+    for (int r = 0; r < LA; ++r) {
       const int e = tid + r * DT;
-      int mm, kk;
-      if (TA) {
-        mm = e % DM;
-        kk = e / DM;
-      } else {
-        kk = e % DK;
-        mm = e / DK;
-      }
+      const int mm = TA ? e % DM : e / DK, kk = TA ? e / DM : e % DK;
       const int64_t gm = m0 + mm, gk = k0 + kk;
-      double v = 0.0;
-      if (gm < M && gk < K) v = TA ? A[gk * lda + gm] : A[gm * lda + gk];
-      const float h = float(v);
-      Ah[kk][mm] = h;
-      Al[kk][mm] = float(v - double(h));
+      pa[r] = (gm < M && gk < K) ? (TA ? A[gk * lda + gm] : A[gm * lda + gk]) : 0.0;
     }
 #pragma unroll
-    for (int r = 0; r < (DN * DK) / DT; ++r) {
+    for (int r = 0; r < LB; ++r) {
       const int e = tid + r * DT;
-      int nn, kk;
-      if (TB) {
-        kk = e % DK;
-        nn = e / DK;
-      } else {
-        nn = e % DN;
-        kk = e / DN;
-      }
+      const int nn = TB ? e / DK : e % DN, kk = TB ? e % DK : e / DN;
       const int64_t gn = n0 + nn, gk = k0 + kk;
-      double v = 0.0;
-      if (gn < N && gk < K) v = TB ? B[gn * ldb + gk] : B[gk * ldb + gn];
-      const float h = float(v);
-      Bh[kk][nn] = h;
-      Bl[kk][nn] = float(v - double(h));
+      pb[r] = (gn < N && gk < K) ? (TB ? B[gn * ldb + gk] : B[gk * ldb + gn]) : 0.0;
     }
-    __syncthreads();
+  };
+  // registers -> shared memory as (hi, lo) float pairs
+  auto stage = [&]() {
+#pragma unroll
+    for (int r = 0; r < LA; ++r) {
+      const int e = tid + r * DT;
+      const int mm = TA ? e % DM : e / DK, kk = TA ? e / DM : e % DK;
+      split_df(pa[r], Ah[kk][mm], Al[kk][mm]);
+    }
+#pragma unroll
+    for (int r = 0; r < LB; ++r) {
+      const int e = tid + r * DT;
+      const int nn = TB ? e / DK : e % DN, kk = TB ? e % DK : e / DN;
+      split_df(pb[r], Bh[kk][nn], Bl[kk][nn]);
+    }
+  };
+  // software pipeline: the global loads of slab k0 + DK are in flight while slab k0 is multiplied
+  fetch(0);
+  stage();
+  __syncthreads();
+  for (int64_t k0 = 0; k0 < K; k0 += DK) {
+    const bool more = k0 + DK < K;
+    if (more) fetch(k0 + DK);
 #pragma unroll 2
     for (int kk = 0; kk < DK; ++kk) {
       float ah[RI], al[RI], bh[RJ], bl[RJ];
@@ -112,6 +151,10 @@ __global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int
         for (int j = 0; j < RJ; ++j) df_fma(ah[i], al[i], bh[j], bl[j], ch[i][j], cl[i][j]);
     }
     __syncthreads();
+    if (more) {
+      stage();
+      __syncthreads();
+    }
   }
 #pragma unroll
   for (int i = 0; i < RI; ++i) {

@@ -430,7 +430,7 @@ struct QrWs {
 constexpr int QBMAX = 64;  // widest panel
 constexpr int QR_SPLIT_MAX = 16;
 inline int qr_nsplit(int64_t k) {
-  int64_t s = (k + 255) / 256;
+  int64_t s = (k + 127) / 128;
   return int(s < 1 ? 1 : (s > QR_SPLIT_MAX ? QR_SPLIT_MAX : s));
 }
 
@@ -590,14 +590,15 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
     if (nc > 0) {
       panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, w.Vp);
       TNX_LAUNCH_CHECK();
-      double* C = w.F + (j0 + nb) * m + j0;  // column-major mp x nc, ld m
-      // W1^T (nc x nb) = C^T V  (thin output, long K: split over K)
-      TNX_TRY(gemm_f64_splitk(false, true, nc, nb, mp, 1.0, C, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
+      // Row-major views: C (column-major mp x nc, ld m) is C^T (nc x mp, ld m), V is V^T (nb x mp).
+      double* C = w.F + (j0 + nb) * m + j0;
+      // W1 (nb x nc) = V^T C  (short output rows, long K: split over K)
+      TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, w.Vp, mp, C, m, 0.0, w.W1, nc, qr_nsplit(mp), w.part,
                               st, df));
-      // W2^T = W1^T T   (T column-major with ld NB == row-major T^T)
-      TNX_TRY(gemm_fp64_class(df, false, true, nc, nb, nb, 1.0, w.W1, nb, 0, Tp, NB, 0, 0.0, w.W2, nb, 0, 1, st));
-      // C^T -= W2^T V^T
-      TNX_TRY(gemm_fp64_class(df, false, false, nc, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, C, m, 0, 1, st));
+      // W2 = T^T W1   (T column-major with ld NB is T^T row-major)
+      TNX_TRY(gemm_fp64_class(df, false, false, nb, nc, nb, 1.0, Tp, NB, 0, w.W1, nc, 0, 0.0, w.W2, nc, 0, 1, st));
+      // C -= V W2, i.e. C^T -= W2^T V^T
+      TNX_TRY(gemm_fp64_class(df, true, false, nc, mp, nb, -1.0, w.W2, nc, 0, w.Vp, mp, 0, 1.0, C, m, 0, 1, st));
     }
   }
   // Q = H_0 H_1 ... [I; 0]: apply panels last to first to the columns >= j0
@@ -611,13 +612,13 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
     panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, w.Vp);
     TNX_LAUNCH_CHECK();
     double* Qs = w.Qc + j0 * m + j0;  // column-major mp x nq, ld m
-    // W1^T (nq x nb) = Qs^T V
-    TNX_TRY(gemm_f64_splitk(false, true, nq, nb, mp, 1.0, Qs, m, w.Vp, mp, 0.0, w.W1, nb, qr_nsplit(mp), w.part,
+    // W1 (nb x nq) = V^T Qs
+    TNX_TRY(gemm_f64_splitk(false, true, nb, nq, mp, 1.0, w.Vp, mp, Qs, m, 0.0, w.W1, nq, qr_nsplit(mp), w.part,
                             st, df));
-    // W2^T = W1^T T^T  -> B = T^T: op(B)[k][n] = T[n][k] = Tcm[k*NB + n] -> row-major, ld NB
-    TNX_TRY(gemm_fp64_class(df, false, false, nq, nb, nb, 1.0, w.W1, nb, 0, Tp, NB, 0, 0.0, w.W2, nb, 0, 1, st));
-    // Qs^T -= W2^T V^T
-    TNX_TRY(gemm_fp64_class(df, false, false, nq, mp, nb, -1.0, w.W2, nb, 0, w.Vp, mp, 0, 1.0, Qs, m, 0, 1, st));
+    // W2 = T W1   (op(A) = T: the row-major view of column-major T is T^T, so transpose it)
+    TNX_TRY(gemm_fp64_class(df, true, false, nb, nq, nb, 1.0, Tp, NB, 0, w.W1, nq, 0, 0.0, w.W2, nq, 0, 1, st));
+    // Qs -= V W2
+    TNX_TRY(gemm_fp64_class(df, true, false, nq, mp, nb, -1.0, w.W2, nq, 0, w.Vp, mp, 0, 1.0, Qs, m, 0, 1, st));
   }
   return TNX_OK;
 }

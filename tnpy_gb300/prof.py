@@ -5,6 +5,7 @@
     python -m tnpy_gb300.prof qr --m 2048 --n 1024   # Householder QR (cluster panel), FP64 GEMMs
     python -m tnpy_gb300.prof gauge --chi 1024       # one-site gauge move (QR with double-FP32 GEMMs)
     python -m tnpy_gb300.prof davidson --chi 512     # one mixed-precision local eigensolve
+    python -m tnpy_gb300.prof sweep --chi 1024 --sites 100   # fDMRG sweeps of XXZ(n, -0.5), per family
 
 Each mode runs two warm-up calls and then --reps calls of the same shapes, on random seeded
 inputs, and prints the CUDA-event time per call and its split over the library's kernel
@@ -58,7 +59,9 @@ def _fmt(fam):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("mode", choices=["matvec", "env", "qr", "gauge", "davidson"])
+    p.add_argument("mode", choices=["matvec", "env", "qr", "gauge", "davidson", "sweep"])
+    p.add_argument("--sites", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--chi", type=int, default=1024)
     p.add_argument("--m", type=int, default=2048)
     p.add_argument("--n", type=int, default=1024)
@@ -68,6 +71,24 @@ def main(argv=None):
     g = torch.Generator(device="cpu").manual_seed(0)
     rnd = lambda *shape: torch.randn(*shape, generator=g, dtype=torch.float64).to(dev)  # noqa: E731
     chi = a.chi
+    if a.mode == "sweep":
+        import tnpy_gb300 as tg
+
+        f = tg.FiniteDMRG(tg.model.XXZ(a.sites, -0.5).mpo, bond_dim=chi, precision="mixed", seed=1234,
+                          compute_variance=False, device=dev)
+        dirs = [tg.Direction.RIGHTWARD, tg.Direction.LEFTWARD]
+        step = [0]
+
+        def sweep():
+            f.sweep(dirs[step[0] % 2], tol=1e-8)
+            step[0] += 1
+
+        for _ in range(a.warmup):
+            sweep()
+        t = _time(sweep, a.reps)
+        fam = _families(sweep, 1)
+        print(f"sweep XXZ({a.sites}) chi={chi}: {t:.1f} ms per sweep; one sweep per family: " + _fmt(fam))
+        return
     if a.mode in ("matvec", "env", "davidson"):
         L, R, W, x = rnd(chi, 5, chi), rnd(chi, 5, chi), rnd(5, 5, 2, 2), rnd(chi, 2, chi)
         L = 0.5 * (L + L.permute(2, 1, 0))
