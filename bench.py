@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the matvec-form and tSDRG measurements")
     p.add_argument("--tsdrg-realizations", type=int, default=64)
+    p.add_argument("--chains", type=int, default=64, help="independent chi=64 chains of the batched fDMRG line")
     return p.parse_args()
 
 
@@ -201,11 +202,17 @@ def tsdrg_rate(n_real: int, with_cpu: bool):
     tg.BatchedTSDRG(mpos[:2], chi=chi).run()  # warm-up (kernels, workspaces)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b = tg.BatchedTSDRG(mpos, chi=chi).run()
+    b = tg.BatchedTSDRG(mpos, chi=chi).run()  # FP64 (the reference's arithmetic)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bm = tg.BatchedTSDRG(mpos, chi=chi, precision="mixed").run()
+    torch.cuda.synchronize()
+    dtm = time.perf_counter() - t0
     out = {"workload": f"tsdrg_random_coupling_n{n}_chi{chi}_delta1_h0", "realizations": n_real,
-           "value": n_real / dt, "unit": "realizations/s", "seconds": dt, "e0_realization0": float(b.evals[0][0]),
+           "value": n_real / dt, "unit": "realizations/s", "precision": "fp64", "seconds": dt,
+           "mixed": {"value": n_real / dtm, "seconds": dtm, "e0_realization0": float(bm.evals[0][0])},
+           "e0_realization0": float(b.evals[0][0]),
            "note": "h=0 is SU(2) symmetric: chi=32 cuts through degenerate multiplets, so the kept states "
                    "(and the variational energy) depend on rounding in any implementation"}
     if with_cpu:
@@ -218,6 +225,42 @@ def tsdrg_rate(n_real: int, with_cpu: bool):
         tc = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": 1.0 / tc, "unit": "realizations/s", "cores": os.cpu_count(),
                                "kind": "port", "sample": "one realisation (r=0) of the numpy restatement"}
+    return out
+
+
+def chains_rate(n_chains: int, with_cpu: bool, workers: int = 16):
+    """Independent chains RandomHeisenberg(64, h=1, seed=100+c) at chi=64 swept concurrently
+    (BatchedFiniteDMRG: one CUDA stream per host worker), to convergence (|dE| < 1e-8, at most 8
+    sweeps). Reported as chain-sweeps/s, with one sweep of one chain of the CPU restatement
+    timed beside it."""
+    import torch
+
+    import tnpy_gb300 as tg
+
+    n, chi = 64, 64
+    mpos = [tg.model.RandomHeisenberg(n, h=1.0, seed=100 + c).mpo for c in range(n_chains)]
+    tg.BatchedFiniteDMRG(mpos[:2], bond_dim=chi, workers=2, compute_variance=False).run(tol=1e-8, max_sweep=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = tg.BatchedFiniteDMRG(mpos, bond_dim=chi, workers=workers, compute_variance=False)
+    b.run(tol=1e-8, max_sweep=8)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    sweeps = sum(b.sweeps)
+    out = {"workload": f"fdmrg_random_heisenberg_n{n}_chi{chi}_h1_chains{n_chains}", "chains": n_chains,
+           "workers": workers, "precision": "fp64", "value": sweeps / dt, "unit": "chain-sweeps/s",
+           "chains_per_s": n_chains / dt, "sweeps_total": sweeps, "seconds": dt,
+           "e0_chain0": float(b.energies[0][-1])}
+    if with_cpu:
+        from oracle import dmrg as odmrg
+        from oracle import models as om
+
+        o = odmrg.FiniteDMRG(om.random_heisenberg_mpo(n, 1.0, seed=100), chi=chi)
+        t0 = time.perf_counter()
+        o.sweep(True, 1e-8)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / tc, "unit": "chain-sweeps/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "first (rightward) sweep of chain 0 of the numpy restatement"}
     return out
 
 
@@ -353,6 +396,7 @@ def run_ours(a):
     if rank == 0 and not a.no_extras:
         line["matvec_forms"] = matvec_forms(f, a.n // 2)
         line["tsdrg"] = tsdrg_rate(a.tsdrg_realizations, with_cpu=(world == 1 and not a.no_cpu))
+        line["chains"] = chains_rate(a.chains, with_cpu=(world == 1 and not a.no_cpu))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

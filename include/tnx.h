@@ -175,7 +175,9 @@ int tnx_tsdrg_project(const double* const* w1, const double* const* w2, const do
  * block. meta[5b..5b+4] = m1, m2, dr2, k, p (node dimensions m1, m2 <= 32, k kept pairs,
  * p = subspace size with k <= p <= min(m1 m2, 48)); D <= 6; keep >= every k.
  * evals: batch x keep; evecs: batch x (max_m x keep) row-major, like tnx_eigh_batched;
- * iters (device, may be null): filter iterations per block. */
+ * iters (device, may be null): filter iterations per block, or a negative count for a block
+ * whose wanted residuals did not reach the tolerance within the iteration limit (its pairs are
+ * then approximate; callers re-solve such blocks densely). */
 size_t tnx_tsdrg_block_eigh_workspace_bytes(int batch, int max_m, int keep, int precision);
 int tnx_tsdrg_block_eigh(const double* const* w1, const double* const* w2, const int* meta, int D,
                          int batch, int max_m, int keep, int precision, double* evals,

@@ -242,3 +242,42 @@ def test_gauge_move_df64(cuda):
     m = a2.reshape(-1, 128)
     np.testing.assert_allclose(m.T @ m, np.eye(128), atol=1e-12)
     np.testing.assert_allclose(np.tensordot(a2, nb2, axes=([2], [0])), two, atol=1e-11)
+
+
+@pytest.mark.parametrize("direction", [1, -1])
+def test_gauge_move_df64_rank_deficient(cuda, direction):
+    """chi=512 gauge move in the FP64-class (double-FP32) form on a site tensor whose Schmidt
+    values span 20 decades, as converged MPS bonds do: Q stays orthonormal to 1e-12 and the
+    two-site product is reproduced to 1e-11 of its norm."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(5)
+    chi, d = 512, 2
+    if direction == 1:
+        m, n = chi * d, chi
+    else:
+        m, n = chi * d, chi
+    u, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    v, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = 10.0 ** (-np.linspace(0, 20, n))
+    psi = (u * s) @ v.T  # m x n, numerically rank deficient
+    if direction == 1:
+        a = psi.reshape(chi, d, chi)
+        nb = rng.standard_normal((chi, d, 64))
+        two = np.tensordot(a, nb, axes=([2], [0]))
+    else:
+        a = psi.T.reshape(chi, d, chi)  # (chi_l) x (d chi_r)
+        nb = rng.standard_normal((64, d, chi))
+        two = np.tensordot(nb, a, axes=([2], [0]))
+    ta, tn = _t(a, cuda), _t(nb, cuda)
+    K.gauge_move(direction, ta, tn, precision="mixed")
+    a2, nb2 = ta.cpu().numpy(), tn.cpu().numpy()
+    if direction == 1:
+        q = a2.reshape(-1, chi)
+        np.testing.assert_allclose(q.T @ q, np.eye(chi), atol=1e-12)
+        back = np.tensordot(a2, nb2, axes=([2], [0]))
+    else:
+        q = a2.reshape(chi, -1)
+        np.testing.assert_allclose(q @ q.T, np.eye(chi), atol=1e-12)
+        back = np.tensordot(nb2, a2, axes=([2], [0]))
+    assert np.max(np.abs(back - two)) <= 1e-11 * np.max(np.abs(two))

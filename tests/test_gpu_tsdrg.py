@@ -111,7 +111,8 @@ def test_kronecker_eigensolver(cuda, precision, m1, m2, dl, dr, chi):
     h = ots.block_hamiltonian(w1, w2)
     w, v = np.linalg.eigh(h)
     t1, t2 = torch.from_numpy(w1).to(cuda), torch.from_numpy(w2).to(cuda)
-    ev, vec, ks = kron_eigh([(t1, t2)], chi, cuda, precision=precision)
+    ev, vec, ks, iters = kron_eigh([(t1, t2)], chi, cuda, precision=precision)
+    assert int(iters[0]) > 0, "subspace iteration reported no convergence"
     k = ks[0]
     ev, vec = ev.cpu().numpy()[0, :k], vec.cpu().numpy()[0, : m1 * m2, :k]
     np.testing.assert_allclose(ev, w[:k], atol=1e-10 * max(1.0, np.abs(w).max()))
@@ -130,5 +131,20 @@ def test_chain_kronecker_path_vs_oracle(cuda):
     t.run()
     o = ots.TreeTensorNetworkSDRG(_oracle_chain(n, seed, 0.5), chi).run()
     np.testing.assert_allclose(t.evals, o.evals, atol=1e-10)
+    assert [[n_.left.node_id, n_.right.node_id, n_.node_id] for n_ in t.tree if not n_.is_leaf] == \
+        [list(m) for m in o.merges]
+
+
+def test_chain_n64_chi32_fp64_vs_oracle(cuda):
+    """chi = 32 on 64 sites: blocks of up to 1024 states with clustered spectra, solved by the
+    two-stage (FP32 then FP64) Kronecker subspace iteration; same merges and energies as the
+    numpy eigh restatement."""
+    import tnpy_gb300 as tg
+
+    n, chi, seed = 64, 32, 10001
+    t = tg.TSDRG(tg.model.RandomCouplingHeisenberg(n, delta=1.0, h=0.5, seed=seed).mpo, chi=chi)
+    t.run()
+    o = ots.TreeTensorNetworkSDRG(_oracle_chain(n, seed, 0.5), chi).run()
+    np.testing.assert_allclose(t.evals, o.evals, atol=1e-9 * np.abs(o.evals).max())
     assert [[n_.left.node_id, n_.right.node_id, n_.node_id] for n_ in t.tree if not n_.is_leaf] == \
         [list(m) for m in o.merges]

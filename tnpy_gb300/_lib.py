@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import threading
 from pathlib import Path
 
 import torch
@@ -122,19 +123,27 @@ def stream_ptr(stream: torch.cuda.Stream | None = None) -> int:
 
 
 class Workspace:
-    """Per-device scratch buffer grown on demand (torch caching allocator)."""
+    """Scratch buffer per (device, stream), grown on demand (torch caching allocator).
 
-    _bufs: dict[int, torch.Tensor] = {}
+    Library calls on different streams must not share scratch, so host threads that drive
+    independent chains on their own streams (``BatchedFiniteDMRG``) each get their own buffer;
+    the buffer is allocated while its stream is current, so the caching allocator orders its
+    reuse on that stream."""
+
+    _bufs: dict[tuple[int, int], torch.Tensor] = {}
+    _lock = threading.Lock()
 
     @classmethod
     def get(cls, nbytes: int, device: torch.device) -> tuple[int, int]:
         idx = device.index if device.index is not None else torch.cuda.current_device()
-        buf = cls._bufs.get(idx)
-        if buf is None or buf.numel() < nbytes:
-            if buf is not None:
-                del cls._bufs[idx]
-                del buf
-            size = max(int(nbytes * 1.25), 1 << 20)
-            buf = torch.empty(size, dtype=torch.uint8, device=torch.device("cuda", idx))
-            cls._bufs[idx] = buf
-        return buf.data_ptr(), buf.numel()
+        key = (idx, torch.cuda.current_stream(idx).cuda_stream)
+        with cls._lock:
+            buf = cls._bufs.get(key)
+            if buf is None or buf.numel() < nbytes:
+                if buf is not None:
+                    del cls._bufs[key]
+                    del buf
+                size = max(int(nbytes * 1.25), 1 << 20)
+                buf = torch.empty(size, dtype=torch.uint8, device=torch.device("cuda", idx))
+                cls._bufs[key] = buf
+            return buf.data_ptr(), buf.numel()

@@ -9,6 +9,8 @@
 // independent, so all threads of the CTA work on one round at a time.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "tnx_internal.cuh"
 
 namespace tnx {
@@ -396,11 +398,11 @@ int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cu
     set_error("rr_lowest_f64: n=%d > %d", n, RW_MAX);
     return TNX_ERR_SHAPE;
   }
-  static bool attr = false;
+  static std::atomic<bool> attr{false};  // idempotent setup; threads may race to it
   const size_t smem = rr_lowest_smem(RW_MAX);
-  if (!attr) {
+  if (!attr.load()) {
     TNX_CUDA(cudaFuncSetAttribute(rr_lowest_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    attr = true;
+    attr.store(true);
   }
   profile_mark(KF_EIGH, st, true);
   rr_lowest_warp_kernel<<<1, RR_T, rr_lowest_smem(n), st>>>(A, n, ld, eval, evec);

@@ -32,41 +32,6 @@ __device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, f
   cl += err + e;
 }
 
-// x = hi + lo with |x - hi - lo| < 2^-47 |x| for 2^-100 < |x| < FLT_MAX: hi is x truncated to
-// 24 significant bits, lo the remaining 29 mantissa bits truncated to 24 (a float denormal
-// when it falls below 2^-126). Integer operations only: the split takes no FP64-pipe issue
-// slots (float(x - double(float(x))) costs a DADD and two conversions on that pipe). Zero and
-// |x| < 2^-126 give (+-0, +-0); |x| > FLT_MAX gives (+-inf, 0), NaN gives (NaN, 0).
-__device__ __forceinline__ void split_df(double x, float& hi, float& lo) {
-  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned hw = unsigned(u >> 32), lw = unsigned(u);
-  const unsigned sign = hw & 0x80000000u;
-  const int e = int((hw >> 20) & 0x7ffu);
-  const int fe = e - 896;  // float exponent field: e - 1023 + 127
-  const unsigned m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
-  const unsigned r29 = lw & 0x1fffffffu;
-  if (fe <= 0) {
-    hi = __uint_as_float(sign);
-    lo = hi;
-    return;
-  }
-  if (fe >= 255) {
-    hi = __uint_as_float(sign | 0x7f800000u | ((e == 2047 && (m23 | r29)) ? 0x400000u : 0u));
-    lo = 0.f;
-    return;
-  }
-  hi = __uint_as_float(sign | (unsigned(fe) << 23) | m23);
-  unsigned lb = sign;
-  if (r29 != 0u) {
-    const int p = 31 - __clz(r29);  // leading one of the remainder
-    const unsigned full = p >= 23 ? (r29 >> (p - 23)) : (r29 << (23 - p));
-    const int le = e - 948 + p;  // float exponent field of lo: (e - 1075 + p) + 127
-    if (le > 0) lb |= (unsigned(le) << 23) | (full & 0x7fffffu);
-    else if (1 - le < 24) lb |= full >> (1 - le);
-  }
-  lo = __uint_as_float(lb);
-}
-
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int64_t K, double alpha,
                                                      const double* __restrict__ A, int64_t lda, int64_t sa,

@@ -25,6 +25,8 @@
 
 #include <cstring>
 
+#include <atomic>
+
 #include "tnx_internal.cuh"
 
 namespace tnx {
@@ -388,10 +390,10 @@ int launch_gemm(const __nv_bfloat16* a_hi, const __nv_bfloat16* a_lo, const __nv
   TNX_TRY(make_map(&mbh, b_hi, N, Kp, BN));
   TNX_TRY(make_map(&mbl, b_lo, N, Kp, BN));
   const size_t smem = gemm_smem_bytes<BN>();
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::atomic<bool> attr_set{false};  // idempotent setup; threads may race to it
+  if (!attr_set.load()) {
     TNX_CUDA(cudaFuncSetAttribute(bf16x3_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    attr_set = true;
+    attr_set.store(true);
   }
   dim3 grid(unsigned((N + BN - 1) / BN), unsigned((M + BM - 1) / BM));
   profile_mark(KF_TC_GEMM, st, true);

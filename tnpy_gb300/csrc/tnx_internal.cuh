@@ -81,6 +81,88 @@ struct Arena {
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
+// ---- double-FP32 ("df64") arithmetic helpers ----------------------------------------
+// x = hi + lo with |x - hi - lo| < 2^-47 |x| for 2^-100 < |x| < FLT_MAX: hi is x truncated to
+// 24 significant bits, lo the remaining 29 mantissa bits truncated to 24 (a float denormal
+// when it falls below 2^-126). Integer operations only: the split takes no FP64-pipe issue
+// slots (float(x - double(float(x))) costs a DADD and two conversions on that pipe). Zero and
+// |x| < 2^-126 give (+-0, +-0); |x| > FLT_MAX gives (+-inf, 0), NaN gives (NaN, 0).
+__device__ __forceinline__ void split_df(double x, float& hi, float& lo) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned hw = unsigned(u >> 32), lw = unsigned(u);
+  const unsigned sign = hw & 0x80000000u;
+  const int e = int((hw >> 20) & 0x7ffu);
+  const int fe = e - 896;  // float exponent field: e - 1023 + 127
+  const unsigned m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
+  const unsigned r29 = lw & 0x1fffffffu;
+  if (fe <= 0) {
+    hi = __uint_as_float(sign);
+    lo = hi;
+    return;
+  }
+  if (fe >= 255) {
+    hi = __uint_as_float(sign | 0x7f800000u | ((e == 2047 && (m23 | r29)) ? 0x400000u : 0u));
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | (unsigned(fe) << 23) | m23);
+  unsigned lb = sign;
+  if (r29 != 0u) {
+    const int p = 31 - __clz(r29);  // leading one of the remainder
+    const unsigned full = p >= 23 ? (r29 >> (p - 23)) : (r29 << (23 - p));
+    const int le = e - 948 + p;  // float exponent field of lo: (e - 1075 + p) + 127
+    if (le > 0) lb |= (unsigned(le) << 23) | (full & 0x7fffffu);
+    else if (1 - le < 24) lb |= full >> (1 - le);
+  }
+  lo = __uint_as_float(lb);
+}
+
+// (h, l) -> the nearest double of h + l (two conversions and one FP64 add)
+__device__ __forceinline__ double join_df(float h, float l) { return double(h) + double(l); }
+
+// s + e = a + b exactly (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (rh, rl) = (xh, xl) - (wh, wl) * (vh, vl), renormalised (|rl| <= ulp(rh) / 2)
+__device__ __forceinline__ void df_fms(float xh, float xl, float wh, float wl, float vh, float vl, float& rh,
+                                       float& rl) {
+  const float p = wh * vh;
+  float pe = fmaf(wh, vh, -p);
+  pe = fmaf(wh, vl, pe);
+  pe = fmaf(wl, vh, pe);
+  float s, e;
+  two_sum_f(xh, -p, s, e);
+  e += xl - pe;
+  rh = s + e;
+  rl = e - (rh - s);
+}
+
+// (rh, rl) = (ah, al) * (bh, bl), renormalised
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& rh, float& rl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  rh = p + e;
+  rl = e - (rh - p);
+}
+
+// (ch, cl) += (ah, al) * (bh, bl), cl left unnormalised (accumulators of long sums)
+__device__ __forceinline__ void df_fma_acc(float ah, float al, float bh, float bl, float& ch, float& cl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  float s, err;
+  two_sum_f(ch, p, s, err);
+  ch = s;
+  cl += err + e;
+}
+
 // ---- FP64 GEMM (row-major, optional transposes, strided batch) --------------------
 // k_total > 0 selects split-K: batch z multiplies the K slice [z*k, min((z+1)*k, k_total))
 int gemm_f64(bool trans_a, bool trans_b, int64_t m, int64_t n, int64_t k, double alpha,

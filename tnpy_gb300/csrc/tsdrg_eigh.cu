@@ -11,12 +11,17 @@
 //      vectors: Rayleigh-Ritz with a one-warp Jacobi of the p x p projected matrix, a degree-q
 //      Chebyshev filter damping [theta_p, upper bound], CGS2 orthonormalisation; stop when the
 //      k wanted residuals reach T's rounding level.
+//      In FP64 precision the FP32 iteration runs first and the FP64 iteration starts from its
+//      k vectors, so the slow FP64 pipe only takes the last digits (a few outer iterations).
+//      The filter's upper bound comes from 24 Lanczos steps (largest Ritz value + |beta|).
 //   2. FP64 Rayleigh-Ritz refinement of the k kept vectors (kron_refine_kernel): CGS2 in FP64,
 //      Z = H V in FP64, G = V^T Z, FP64 Jacobi of G, V <- V Q. Ritz values are second order in
 //      the subspace error, so an FP32 subspace (~1e-6) gives FP64-accurate kept spectra.
 //
 // Work vectors live in global memory (L2-resident): 4 p m values of T per CTA.
 #include <cuda_runtime.h>
+
+#include <atomic>
 
 #include "tnx_internal.cuh"
 
@@ -47,6 +52,44 @@ template <typename T>
 __device__ __forceinline__ T wsum(T v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// a . b over m entries, returned to every thread
+template <typename T>
+__device__ T dot1(KSmem<T>& s, const T* a, const T* b, int m) {
+  T part = T(0);
+  for (int e = threadIdx.x; e < m; e += KT) part += a[e] * b[e];
+  part = wsum(part);
+  if ((threadIdx.x & 31) == 0) s.red[threadIdx.x >> 5][0] = part;
+  __syncthreads();
+  T t = T(0);
+  for (int q = 0; q < KT / 32; ++q) t += s.red[q][0];
+  __syncthreads();
+  return t;
+}
+
+// largest eigenvalue of the symmetric tridiagonal (alpha[0..n), beta[1..n)) by Sturm bisection
+__device__ double tridiag_max(const double* alpha, const double* beta, int n) {
+  double lo = alpha[0], hi = alpha[0];
+  for (int i = 0; i < n; ++i) {  // Gershgorin interval
+    const double r = (i > 0 ? fabs(beta[i]) : 0.0) + (i + 1 < n ? fabs(beta[i + 1]) : 0.0);
+    lo = fmin(lo, alpha[i] - r);
+    hi = fmax(hi, alpha[i] + r);
+  }
+  for (int it = 0; it < 60; ++it) {
+    const double x = 0.5 * (lo + hi);
+    int below = 0;  // eigenvalues < x
+    double q = alpha[0] - x;
+    below += q < 0.0;
+    for (int i = 1; i < n; ++i) {
+      if (q == 0.0) q = 1e-300;
+      q = alpha[i] - x - beta[i] * beta[i] / q;
+      below += q < 0.0;
+    }
+    if (below == n) hi = x;  // every eigenvalue below x
+    else lo = x;
+  }
+  return hi;
 }
 
 // Y[:, j] = H X[:, j] for j < ncols (vector-major storage [j][m]).
@@ -249,7 +292,7 @@ __global__ void __launch_bounds__(KT) kron_chfsi_kernel(const double* const* __r
                                                        const int* __restrict__ meta, int D, T* __restrict__ work,
                                                        int64_t work_stride, int max_outer, int degree,
                                                        double* __restrict__ vec_base, int64_t vec_stride,
-                                                       int* __restrict__ out_iters) {
+                                                       int* __restrict__ out_iters, int warm) {
   extern __shared__ __align__(16) unsigned char ksm_raw[];
   KSmem<T>& s = *reinterpret_cast<KSmem<T>*>(ksm_raw);
   const int b = blockIdx.x;
@@ -283,12 +326,71 @@ __global__ void __launch_bounds__(KT) kron_chfsi_kernel(const double* const* __r
     s.scal[KP - 1] = bound;
   }
   __syncthreads();
-  const T ub = s.scal[KP - 1] * T(1.01) + T(1e-30);
   T* X = work + size_t(b) * work_stride;
   T* Y = X + size_t(p) * m;
   T* Z = Y + size_t(p) * m;
   T* U = Z + size_t(p) * m;
-  for (int e = threadIdx.x; e < p * m; e += KT) X[e] = T(hash_unit(b, e / m, e % m));
+  // Upper end of the spectrum for the filter: 24 Lanczos steps on one vector give the largest
+  // Ritz value theta_max; theta_max + |beta_last| (plus 1% of the Ritz range) bounds lambda_max
+  // in practice and is far tighter than the norm bound, which caps it. A tighter damping
+  // interval makes every filter application converge faster.
+  T ub;
+  {
+    __shared__ double lal[25], lbe[25];
+    const int nl = m < 24 ? m : 24;
+    T* v = X;
+    T* vp = X + m;
+    T* w = Y;
+    for (int e = threadIdx.x; e < m; e += KT) {
+      v[e] = T(hash_unit(b + 7919u, 0u, uint32_t(e)));
+      vp[e] = T(0);
+    }
+    __syncthreads();
+    T nv = sqrt(dot1(s, v, v, m));
+    for (int e = threadIdx.x; e < m; e += KT) v[e] /= nv;
+    __syncthreads();
+    T beta = T(0);
+    int steps = 0;
+    for (int j = 0; j < nl; ++j) {
+      kron_apply(s, v, w, 1, m1, m2, D);
+      const T alpha = dot1(s, w, v, m);
+      for (int e = threadIdx.x; e < m; e += KT) w[e] -= alpha * v[e] + beta * vp[e];
+      __syncthreads();
+      const T bnew = sqrt(dot1(s, w, w, m));
+      if (threadIdx.x == 0) {
+        lal[j] = double(alpha);
+        lbe[j + 1] = double(bnew);
+      }
+      steps = j + 1;
+      if (!(bnew > T(1e-12) * (abs(alpha) + T(1e-30)))) break;
+      for (int e = threadIdx.x; e < m; e += KT) {
+        vp[e] = v[e];
+        v[e] = w[e] / bnew;
+      }
+      beta = bnew;
+      __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      lbe[0] = 0.0;
+      double tmin = lal[0], tmax = lal[0];
+      for (int i = 0; i < steps; ++i) {
+        tmin = fmin(tmin, lal[i]);
+        tmax = fmax(tmax, lal[i]);
+      }
+      const double top = tridiag_max(lal, lbe, steps);
+      double est = top + fabs(lbe[steps]) + 0.01 * fabs(top - tmin) + 1e-12 * fabs(top);
+      const double cap = double(s.scal[KP - 1]) * 1.01;
+      s.scal[KP - 2] = T(est < cap ? est : cap);
+    }
+    __syncthreads();
+    ub = s.scal[KP - 2] + T(1e-30);
+  }
+  // start block: random, or (warm) the k vectors a previous stage left in vec_base plus random
+  // guard vectors
+  const double* prev = vec_base + size_t(b) * vec_stride;
+  for (int e = threadIdx.x; e < p * m; e += KT)
+    X[e] = (warm && e < k * m) ? T(prev[e]) : T(hash_unit(b, e / m, e % m));
   __syncthreads();
   orthonormalise(s, X, p, m);
   const T tolr = sizeof(T) == 4 ? T(3e-6) : T(1e-13);
@@ -378,7 +480,8 @@ __global__ void __launch_bounds__(KT) kron_chfsi_kernel(const double* const* __r
   // write the k lowest Ritz vectors (FP64, vector-major [i][m])
   double* out = vec_base + size_t(b) * vec_stride;
   for (int e = threadIdx.x; e < k * m; e += KT) out[e] = double(X[e]);
-  if (threadIdx.x == 0 && out_iters) out_iters[b] = it;
+  // iterations used, or -max_outer when the wanted residuals never reached the tolerance
+  if (threadIdx.x == 0 && out_iters) out_iters[b] = s.flag ? it + 1 : -max_outer;
 }
 
 // FP64 Rayleigh-Ritz of the k vectors in vecs[b] (vector-major [k][m]); writes evals[b][i]
@@ -476,36 +579,48 @@ int tnx_tsdrg_block_eigh(const double* const* w1, const double* const* w2, const
   double* scr = reinterpret_cast<double*>(reinterpret_cast<char*>(vecs) + size_t(batch) * per_vec);
   const int max_outer = 60, degree = 10;
   if (fp64) {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr{false};  // idempotent setup; threads may race to it
+    if (!attr.load()) {
       TNX_CUDA(cudaFuncSetAttribute(kron_chfsi_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(sizeof(KSmem<double>))));
-      attr = true;
+      attr.store(true);
     }
-    profile_mark(KF_EIGH, st, true);
-    kron_chfsi_kernel<double><<<batch, KT, sizeof(KSmem<double>), st>>>(
-        w1, w2, meta, D, reinterpret_cast<double*>(work), int64_t(per_work / 8), max_outer, degree, vecs,
-        int64_t(per_vec / 8), iters);
-    profile_mark(KF_EIGH, st, false);
-  } else {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> fattr{false};  // idempotent setup; threads may race to it
+    if (!fattr.load()) {
       TNX_CUDA(cudaFuncSetAttribute(kron_chfsi_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(sizeof(KSmem<float>))));
-      attr = true;
+      fattr.store(true);
+    }
+    // FP32 iterations to the FP32 rounding level, then FP64 iterations from that subspace:
+    // the FP64 pipe (~2 FMA/clock/SM) only has to take the last digits
+    profile_mark(KF_EIGH, st, true);
+    kron_chfsi_kernel<float><<<batch, KT, sizeof(KSmem<float>), st>>>(
+        w1, w2, meta, D, reinterpret_cast<float*>(work), int64_t(per_work / 4), max_outer, degree, vecs,
+        int64_t(per_vec / 8), nullptr, 0);
+    TNX_LAUNCH_CHECK();
+    kron_chfsi_kernel<double><<<batch, KT, sizeof(KSmem<double>), st>>>(
+        w1, w2, meta, D, reinterpret_cast<double*>(work), int64_t(per_work / 8), max_outer, degree, vecs,
+        int64_t(per_vec / 8), iters, 1);
+    profile_mark(KF_EIGH, st, false);
+  } else {
+    static std::atomic<bool> attr{false};  // idempotent setup; threads may race to it
+    if (!attr.load()) {
+      TNX_CUDA(cudaFuncSetAttribute(kron_chfsi_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(sizeof(KSmem<float>))));
+      attr.store(true);
     }
     profile_mark(KF_EIGH, st, true);
     kron_chfsi_kernel<float><<<batch, KT, sizeof(KSmem<float>), st>>>(
         w1, w2, meta, D, reinterpret_cast<float*>(work), int64_t(per_work / 4), max_outer, degree, vecs,
-        int64_t(per_vec / 8), iters);
+        int64_t(per_vec / 8), iters, 0);
     profile_mark(KF_EIGH, st, false);
   }
   TNX_LAUNCH_CHECK();
-  static bool rattr = false;
-  if (!rattr) {
+  static std::atomic<bool> rattr{false};  // idempotent setup; threads may race to it
+  if (!rattr.load()) {
     TNX_CUDA(cudaFuncSetAttribute(kron_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(sizeof(KSmem<double>))));
-    rattr = true;
+    rattr.store(true);
   }
   kron_refine_kernel<<<batch, KT, sizeof(KSmem<double>), st>>>(w1, w2, meta, D, vecs, int64_t(per_vec / 8), scr,
                                                                int64_t(per_scr / 8), evals, keep, evecs, max_m);

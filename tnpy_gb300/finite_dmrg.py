@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import logging
 import time
+from concurrent.futures import ThreadPoolExecutor
 from enum import Enum
 from itertools import cycle
 
@@ -211,3 +212,76 @@ class FiniteDMRG:
         if len(self._energies) == 1:
             raise RuntimeError("FiniteDMRG is probably not executed yet.")
         return MatrixProductStateMeasurements(self.mps)
+
+
+class BatchedFiniteDMRG:
+    """Many independent chains (disorder realisations, parameter scans) swept concurrently.
+
+    Each chain is a ``FiniteDMRG`` built and swept on its own CUDA stream by one of ``workers``
+    host threads (chain c on worker c mod workers). Every library call releases the GIL and a
+    Davidson solve blocks only the thread that issued it, so the small kernels of different
+    chains overlap on the GPU instead of leaving it idle between launches. Each chain's
+    arithmetic does not depend on the stream it runs on: ``energies[c]`` equals
+    ``FiniteDMRG(mpos[c], bond_dim, **kwargs).run(tol, max_sweep)`` for the same arguments.
+    """
+
+    def __init__(self, mpos, bond_dim: int | None = None, *, chi: int | None = None, workers: int = 8,
+                 device=None, **kwargs):
+        self._mpos = list(mpos)
+        if not self._mpos:
+            raise ValueError("BatchedFiniteDMRG needs at least one MPO")
+        self._bond_dim = bond_dim if bond_dim is not None else chi
+        if self._bond_dim is None:
+            raise TypeError("BatchedFiniteDMRG needs bond_dim (or chi)")
+        self._kwargs = kwargs
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.workers = max(1, min(int(workers), len(self._mpos)))
+        self._streams = [torch.cuda.Stream(self.device) for _ in range(self.workers)]
+        self.chains: list[FiniteDMRG | None] = [None] * len(self._mpos)
+        self.sweeps: list[int] = [0] * len(self._mpos)
+        self._map(self._build)
+
+    def _map(self, fn):
+        def work(w: int):
+            torch.cuda.set_device(self.device)
+            with torch.cuda.stream(self._streams[w]):
+                for c in range(w, len(self._mpos), self.workers):
+                    fn(c)
+            self._streams[w].synchronize()
+
+        with ThreadPoolExecutor(max_workers=self.workers) as ex:
+            for fut in [ex.submit(work, w) for w in range(self.workers)]:
+                fut.result()  # re-raises a chain's exception in the caller
+
+    def _build(self, c: int):
+        self.chains[c] = FiniteDMRG(self._mpos[c], self._bond_dim, device=self.device, **self._kwargs)
+
+    def run(self, tol: float = 1e-8, max_sweep: int = 100, metric: Metric = Metric.ENERGY) -> list[list[float]]:
+        """Sweep every chain until its own |dE| < tol or ``max_sweep`` (FiniteDMRG.run per chain,
+        variance not computed). Returns the per-sweep energies of every chain."""
+
+        def one(c: int):
+            f = self.chains[c]
+            for n_sweep, direction in zip(range(1, max_sweep + 1), cycle([Direction.RIGHTWARD, Direction.LEFTWARD])):
+                f._energies.append(f.sweep(direction, tol=tol))
+                f._variances.append(np.nan)
+                self.sweeps[c] = n_sweep
+                if f._converged(n_sweep, tol, max_sweep, metric):
+                    break
+
+        self._map(one)
+        return self.energies
+
+    def sweep(self, direction: Direction = Direction.RIGHTWARD, tol: float = 1e-8) -> list[float]:
+        """One sweep of every chain in ``direction``; returns each chain's last local energy."""
+        out = [0.0] * len(self._mpos)
+
+        def one(c: int):
+            out[c] = self.chains[c].sweep(direction, tol=tol)
+
+        self._map(one)
+        return out
+
+    @property
+    def energies(self) -> list[list[float]]:
+        return [f.energies for f in self.chains]
