@@ -378,12 +378,25 @@ def run_ours(a):
                              "achieved counts algorithmic flops 2*M*N*K of the unsplit product",
                 "launches": n_l.value, "kernel_ms_total": tot_ms.value,
                 "share_of_step_time": (tot_ms.value / dev_ms) if dev_ms > 0 else None}
+    # FP64-class contractions on the tensor cores (Ozaki GEMM): one further sweep, outside the timed
+    # region, with CUDA events around each of its launches
+    lib.tnx_profile_begin(6)
+    one_sweep()
+    n_o, ms_o, fl_o, by_o = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    lib.tnx_profile_end(ctypes.byref(n_o), ctypes.byref(ms_o), ctypes.byref(fl_o), ctypes.byref(by_o))
+    oz_ach = fl_o.value / (ms_o.value / 1e3) / 1e12 if ms_o.value > 0 else None
+    oz_peak = bf16_sust / 36.0
+    roofline_oz = {"kernel": "oz_gemm_kernel (tcgen05 FP64-class GEMM, 36 exact BF16 slice products)",
+                   "bound": "tensor", "achieved": oz_ach, "peak": oz_peak, "unit": "TFLOP/s",
+                   "frac": (oz_ach / oz_peak) if oz_ach else None, "launches": n_o.value, "kernel_ms_per_sweep": ms_o.value,
+                   "peak_note": "of measured: bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class "
+                                "product); achieved counts algorithmic flops 2*M*N*K"}
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 (split-bf16 tensor-core matvec, FP64 environments / eigensolver)"
             if a.precision == "mixed" else "f64",
             "data": "synthetic (seeded random initial MPS, XXZ MPO)", "config": workload(a),
-            "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+            "roofline": roofline, "roofline_fp64_class": roofline_oz, "clocks": clk, "gpu_launches": int(launches),
             "e2e": {"value": world / e2e_t, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d + 8},
             "energy_last": energies[-1], "wall_s_per_step": wall / a.steps,

@@ -197,6 +197,17 @@ int tnx_gemm_df64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, dou
                   const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
                   int64_t ldc, void* stream);
 
+/* C = alpha * op(A) op(B) + beta * C, row-major FP64, on the tcgen05 tensor cores by exact
+ * integer slicing (Ozaki scheme): rows of op(A) / columns of op(B) scaled by powers of two and
+ * cut into eight 7-bit slices held exactly in BF16, the 36 slice products with s + t < 8
+ * accumulated exactly in FP32 tensor memory over 128-long K chunks and summed in double-FP32.
+ * Error ~2^-52 per product relative to max|row of op(A)| max|column of op(B)|. Returns
+ * TNX_ERR_TIMEOUT if a bounded wait in the kernel expired (synchronises the stream). */
+size_t tnx_gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k);
+int tnx_gemm_oz(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                void* workspace, size_t workspace_bytes, void* stream);
+
 /* C (m x n, row-major FP64) = A (m x k) B^T (B is n x k), both row-major FP64, computed as
  * three BF16 tensor-core products (split-BF16) with FP32 accumulation. Test / building-block
  * entry point of the tcgen05 GEMM used by the mixed-precision matvec. */

@@ -281,3 +281,45 @@ def test_gauge_move_df64_rank_deficient(cuda, direction):
         np.testing.assert_allclose(q @ q.T, np.eye(chi), atol=1e-12)
         back = np.tensordot(nb2, a2, axes=([2], [0]))
     assert np.max(np.abs(back - two)) <= 1e-11 * np.max(np.abs(two))
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("m,n,k", [(128, 64, 128), (300, 200, 500), (1000, 130, 1024), (5, 7, 3), (257, 65, 1500)])
+def test_gemm_oz(cuda, ta, tb, m, n, k):
+    """Ozaki-sliced tensor-core GEMM against the FP64 product on N(0,1) operands: error below
+    1e-13 of sum_k |a_ik| |b_kj|."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(m + n + k)
+    a = rng.standard_normal((k, m) if ta else (m, k))
+    b = rng.standard_normal((n, k) if tb else (k, n))
+    opa, opb = (a.T if ta else a), (b.T if tb else b)
+    ref = opa @ opb
+    bound = np.abs(opa) @ np.abs(opb)
+    got = K.gemm_oz(_t(a, cuda), _t(b, cuda), trans_a=ta, trans_b=tb).cpu().numpy()
+    assert np.max(np.abs(got - ref) / bound) < 1e-13
+
+
+def test_gemm_oz_wide_range(cuda):
+    """Entries spanning ~20 decades: the slicing error is relative to each row's and column's
+    maximum, so the error is bounded by 1e-14 K max|a_i.| max|b_.j|."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(8)
+    m, n, k = 384, 192, 768
+    a = rng.standard_normal((m, k)) * 10.0 ** rng.uniform(-10, 10, (m, k))
+    b = rng.standard_normal((k, n)) * 10.0 ** rng.uniform(-10, 10, (k, n))
+    got = K.gemm_oz(_t(a, cuda), _t(b, cuda)).cpu().numpy()
+    bound = k * np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :]
+    assert np.max(np.abs(got - a @ b) / bound) < 1e-14
+
+
+def test_gemm_oz_exact_small_integers(cuda):
+    """Integer operands below 2^7 make every slice exact: the product is bit-exact."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(3)
+    a = rng.randint(-100, 100, (256, 640)).astype(np.float64)
+    b = rng.randint(-100, 100, (640, 192)).astype(np.float64)
+    got = K.gemm_oz(_t(a, cuda), _t(b, cuda)).cpu().numpy()
+    np.testing.assert_array_equal(got, a @ b)

@@ -74,3 +74,25 @@ def test_fdmrg_mixed_matches_fp64(cuda):
     assert abs(e[-1] - e_ref[-1]) <= 1e-9 * abs(e_ref[-1]), (e[-1], e_ref[-1])
     sz = f.measurements.local_sz()
     assert np.max(np.abs(sz - omps.local_sz(o.mps))) < 1e-4
+
+
+@pytest.mark.parametrize("chi", [128, 256])
+def test_davidson_mixed_from_random_start(cuda, chi):
+    """Local problem of a swept chain solved from a random start vector (far from its ground
+    state): the mixed solver must still converge, to the FP64 solver's eigenvalue."""
+    import torch
+
+    import tnpy_gb300 as tg
+    from tnpy_gb300 import kernels as K
+
+    f = tg.FiniteDMRG(tg.model.XXZ(24, -0.5).mpo, bond_dim=chi, seed=3, compute_variance=False, precision="mixed")
+    f.sweep(tg.Direction.RIGHTWARD, tol=1e-8)
+    site = 12
+    L, W, R = f.env.site_operator(site)
+    shape = f.mps.tensors[site].shape
+    g = torch.Generator(device="cpu").manual_seed(9)
+    x0 = torch.randn(shape, generator=g, dtype=torch.float64).to(cuda)
+    em, rm, itm, okm = K.davidson1(L, W, R, x0.clone(), tol=1e-10, precision="mixed", max_iter=400)
+    ef, rf, itf, okf = K.davidson1(L, W, R, x0.clone(), tol=1e-10, precision="fp64", max_iter=400)
+    assert okm and okf, (em, rm, itm, ef, rf, itf)
+    assert abs(em - ef) <= 1e-9 * abs(ef), (em, ef)

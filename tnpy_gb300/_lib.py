@@ -67,6 +67,9 @@ SIGNATURES = {
     "tnx_gauge_move_workspace_bytes": (_sz, [_int, _i64, _i64, _i64, _i64]),
     "tnx_gauge_move": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _int, _vp, _sz, _vp]),
     "tnx_gemm_df64": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _vp, _i64, _dbl, _vp, _i64, _vp]),
+    "tnx_gemm_oz_workspace_bytes": (_sz, [_i64, _i64, _i64]),
+    "tnx_gemm_oz": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _vp, _i64, _dbl, _vp, _i64, _vp, _sz,
+                           _vp]),
     "tnx_gemm_bf16x3_workspace_bytes": (_sz, [_i64, _i64, _i64]),
     "tnx_gemm_bf16x3": (_int, [_i64, _i64, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tnx_tsdrg_block_hamiltonian": (_int, [_vp, _vp, _vp, _int, _vp, _vp, _int, _int, _vp]),

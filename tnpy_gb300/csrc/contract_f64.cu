@@ -270,16 +270,35 @@ int64_t matvec1_scratch_elems(int64_t chi_l, int64_t d, int64_t chi_r, int64_t d
   return a > b ? a : b;
 }
 
+bool use_oz(int64_t m, int64_t n, int64_t k) {
+  // the tensor-core FP64-class GEMM pays five launches of operand slicing: large products only
+  return m >= 256 && n >= 64 && k >= 128 && double(m) * double(n) * double(k) >= double(1 << 27);
+}
+
+int gemm_fp64_class_oz(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                       int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* oz_ws,
+                       size_t oz_bytes, cudaStream_t st) {
+  if (df && oz_ws && use_oz(m, n, k) && oz_bytes >= gemm_oz_workspace_bytes(m, n, k))
+    return gemm_oz(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, oz_ws, oz_bytes, st);
+  return gemm_fp64_class(df, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+}
+
+size_t matvec1_oz_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr) {
+  size_t a = use_oz(dl * chi_l, d * chi_r, chi_l) ? gemm_oz_workspace_bytes(dl * chi_l, d * chi_r, chi_l) : 0;
+  size_t b = use_oz(chi_l * d, chi_r, chi_r * dr) ? gemm_oz_workspace_bytes(chi_l * d, chi_r, chi_r * dr) : 0;
+  return a > b ? a : b;
+}
+
 int matvec1_f64(const double* L, const double* W, const double* R, const double* x, double* y,
                 int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double* T1,
-                double* T2, cudaStream_t st, bool df) {
+                double* T2, cudaStream_t st, bool df, void* oz_ws, size_t oz_bytes) {
   // T1[(w,a'),(s,c)] = sum_a L[a,(w,a')] x[a,(s,c)]
-  TNX_TRY(gemm_fp64_class(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, L, dl * chi_l, 0, x, d * chi_r, 0,
-                          0.0, T1, d * chi_r, 0, 1, st));
+  TNX_TRY(gemm_fp64_class_oz(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, L, dl * chi_l, x, d * chi_r, 0.0,
+                             T1, d * chi_r, oz_ws, oz_bytes, st));
   TNX_TRY(wcontract_left(T1, W, T2, chi_l, d, chi_r, dl, dr, st));
   // y[(a',s'),c'] = sum_{(c,v)} T2[(a',s'),(c,v)] R[(c,v),c']
-  TNX_TRY(gemm_fp64_class(df, false, false, chi_l * d, chi_r, chi_r * dr, 1.0, T2, chi_r * dr, 0, R, chi_r, 0,
-                          0.0, y, chi_r, 0, 1, st));
+  TNX_TRY(gemm_fp64_class_oz(df, false, false, chi_l * d, chi_r, chi_r * dr, 1.0, T2, chi_r * dr, R, chi_r, 0.0, y,
+                             chi_r, oz_ws, oz_bytes, st));
   return TNX_OK;
 }
 
@@ -351,7 +370,8 @@ size_t tnx_matvec1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int6
                                    int precision) {
   if (precision == TNX_BF16X3 && mixed_supported(chi_l, d, chi_r, dl, dr))
     return matvec1_bf16x3_scratch_bytes(chi_l, d, chi_r, dl, dr);
-  return 2 * align_up(size_t(matvec1_scratch_elems(chi_l, d, chi_r, dl, dr)) * sizeof(double));
+  const size_t t = 2 * align_up(size_t(matvec1_scratch_elems(chi_l, d, chi_r, dl, dr)) * sizeof(double));
+  return precision == TNX_FP64 ? t : t + align_up(matvec1_oz_bytes(chi_l, d, chi_r, dl, dr));
 }
 
 int tnx_matvec1(const double* L, const double* W, const double* R, const double* x, double* y,
@@ -374,7 +394,9 @@ int tnx_matvec1(const double* L, const double* W, const double* R, const double*
   const int64_t ne = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);
   double* T1 = ar.take<double>(ne);
   double* T2 = ar.take<double>(ne);
-  return matvec1_f64(L, W, R, x, y, chi_l, d, chi_r, dl, dr, T1, T2, st, precision == TNX_DF64);
+  const size_t ozb = precision == TNX_DF64 ? matvec1_oz_bytes(chi_l, d, chi_r, dl, dr) : 0;
+  void* oz = ozb ? static_cast<void*>(ar.take<char>(ozb)) : nullptr;
+  return matvec1_f64(L, W, R, x, y, chi_l, d, chi_r, dl, dr, T1, T2, st, precision == TNX_DF64, oz, ozb);
 }
 
 int tnx_diag1(const double* L, const double* W, const double* R, double* diag, int64_t chi_l,
@@ -404,11 +426,30 @@ int tnx_full_matrix1(const double* L, const double* W, const double* R, double* 
   return TNX_OK;
 }
 
+// FP64-class scratch of the environment update's two GEMMs (tensor-core path)
+static size_t env_oz_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr) {
+  int64_t g[2][3];
+  if (direction == 1) {
+    int64_t a[2][3] = {{dl * chi_l, d * chi_r, chi_l}, {chi_r * dr, chi_r, chi_l * d}};
+    memcpy(g, a, sizeof(g));
+  } else {
+    int64_t a[2][3] = {{chi_l * d, dr * chi_r, chi_r}, {chi_l * dl, chi_l, d * chi_r}};
+    memcpy(g, a, sizeof(g));
+  }
+  size_t out = 0;
+  for (auto& x : g)
+    if (use_oz(x[0], x[1], x[2])) {
+      const size_t b = gemm_oz_workspace_bytes(x[0], x[1], x[2]);
+      out = b > out ? b : out;
+    }
+  return out;
+}
+
 size_t tnx_env_update_workspace_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r,
                                       int64_t dl, int64_t dr, int precision) {
-  (void)direction;
-  (void)precision;
-  return 2 * align_up(size_t(matvec1_scratch_elems(chi_l, d, chi_r, dl, dr)) * sizeof(double));
+  const size_t t = 2 * align_up(size_t(matvec1_scratch_elems(chi_l, d, chi_r, dl, dr)) * sizeof(double));
+  if (!use_df64(precision)) return t;
+  return t + align_up(env_oz_bytes(direction == -1 ? -1 : 1, chi_l, d, chi_r, dl, dr));
 }
 
 int tnx_env_update(int direction, const double* E_in, const double* A, const double* W,
@@ -429,22 +470,24 @@ int tnx_env_update(int direction, const double* E_in, const double* A, const dou
   const int64_t ne = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);
   double* T1 = ar.take<double>(ne);
   double* T2 = ar.take<double>(ne);
+  const size_t ozb = df ? env_oz_bytes(direction, chi_l, d, chi_r, dl, dr) : 0;
+  void* oz = ozb ? static_cast<void*>(ar.take<char>(ozb)) : nullptr;
   if (direction == 1) {
     // T1[(w,a'),(s,c)] = sum_a L[a,(w,a')] A[a,(s,c)]
-    TNX_TRY(gemm_fp64_class(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, E_in, dl * chi_l, 0, A, d * chi_r,
-                            0, 0.0, T1, d * chi_r, 0, 1, st));
+    TNX_TRY(gemm_fp64_class_oz(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, E_in, dl * chi_l, A, d * chi_r,
+                               0.0, T1, d * chi_r, oz, ozb, st));
     TNX_TRY(wcontract_left(T1, W, T2, chi_l, d, chi_r, dl, dr, st));
     // L'[(c,v),c'] = sum_{(a',s')} T2[(a',s'),(c,v)] A[(a',s'),c']
-    TNX_TRY(gemm_fp64_class(df, true, false, chi_r * dr, chi_r, chi_l * d, 1.0, T2, chi_r * dr, 0, A, chi_r, 0,
-                            0.0, E_out, chi_r, 0, 1, st));
+    TNX_TRY(gemm_fp64_class_oz(df, true, false, chi_r * dr, chi_r, chi_l * d, 1.0, T2, chi_r * dr, A, chi_r, 0.0,
+                               E_out, chi_r, oz, ozb, st));
   } else {
     // T1[(a,s),(v,c')] = sum_c A[(a,s),c] R[c,(v,c')]
-    TNX_TRY(gemm_fp64_class(df, false, false, chi_l * d, dr * chi_r, chi_r, 1.0, A, chi_r, 0, E_in, dr * chi_r, 0,
-                            0.0, T1, dr * chi_r, 0, 1, st));
+    TNX_TRY(gemm_fp64_class_oz(df, false, false, chi_l * d, dr * chi_r, chi_r, 1.0, A, chi_r, E_in, dr * chi_r,
+                               0.0, T1, dr * chi_r, oz, ozb, st));
     TNX_TRY(wcontract_right(T1, W, T2, chi_l, d, chi_r, dl, dr, st));
     // R'[(a,w),a'] = sum_{(s',c')} T2[(a,w),(s',c')] A[a',(s',c')]
-    TNX_TRY(gemm_fp64_class(df, false, true, chi_l * dl, chi_l, d * chi_r, 1.0, T2, d * chi_r, 0, A, d * chi_r, 0,
-                            0.0, E_out, chi_l, 0, 1, st));
+    TNX_TRY(gemm_fp64_class_oz(df, false, true, chi_l * dl, chi_l, d * chi_r, 1.0, T2, d * chi_r, A, d * chi_r,
+                               0.0, E_out, chi_l, oz, ozb, st));
   }
   return TNX_OK;
 }

@@ -186,7 +186,9 @@ struct DavWs {
   double *V, *AV, *x, *ax, *t, *diag, *Hm, *Hwork, *evals, *evecs, *jwork, *part, *scal;
   void* mv;
   size_t mv_bytes;
-  double *T1, *T2;  // FP64 matvec scratch (also used by the defect correction)
+  double *T1, *T2;  // FP64-class matvec scratch (also used by the anchored phase)
+  void* oz;         // operand slices of the tensor-core FP64-class GEMMs
+  size_t oz_bytes;
 };
 
 size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int mb, int precision,
@@ -196,6 +198,8 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
   const size_t mv_bytes = (precision == TNX_BF16X3 && mixed_supported(chi_l, d, chi_r, dl, dr))
                               ? matvec1_bf16x3_scratch_bytes(chi_l, d, chi_r, dl, dr)
                               : 0;
+  const size_t oz_bytes =
+      (precision == TNX_BF16X3 || precision == TNX_DF64) ? matvec1_oz_bytes(chi_l, d, chi_r, dl, dr) : 0;
   const int nch = nchunk_for(n);
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -207,7 +211,8 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
          oax = take(n * 8), ot = take(n * 8), odiag = take(n * 8), oH = take(size_t(mb) * mb * 8),
          oHw = take(size_t(mb) * mb * 8), oev = take(size_t(mb) * 8), oevec = take(size_t(mb) * mb * 8),
          ojw = take(2 * size_t(mb) * mb * 8), opart = take(size_t(mb + 1) * nch * 8),
-         oscal = take(size_t(4 * MAXB) * 8), oT1 = take(ne * 8), oT2 = take(ne * 8), omv = take(mv_bytes);
+         oscal = take(size_t(4 * MAXB) * 8), oT1 = take(ne * 8), oT2 = take(ne * 8), omv = take(mv_bytes),
+         ooz = take(oz_bytes);
   if (w && base && off <= size) {
     char* b = static_cast<char*>(base);
     w->V = reinterpret_cast<double*>(b + oV);
@@ -227,6 +232,8 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
     w->T2 = reinterpret_cast<double*>(b + oT2);
     w->mv = mv_bytes ? static_cast<void*>(b + omv) : nullptr;
     w->mv_bytes = mv_bytes;
+    w->oz = oz_bytes ? static_cast<void*>(b + ooz) : nullptr;
+    w->oz_bytes = oz_bytes;
   }
   return off;
 }
@@ -268,7 +275,8 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   }
   auto matvec = [&](const double* in, double* out) -> int {
     if (mixed) return mixed_apply(W, in, out, chi_l, d, chi_r, dl, dr, w.mv, st);
-    return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, precision == TNX_DF64);
+    return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, precision == TNX_DF64, w.oz,
+                       w.oz_bytes);
   };
   int hflag = 0;
   double* h = w.scal;               // [MAXB]
@@ -422,7 +430,8 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     converged = false;
     for (int anchor = 0;; ++anchor) {
       TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
-      TNX_TRY(matvec1_f64(L, W, R, w.V, w.AV, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true));
+      TNX_TRY(matvec1_f64(L, W, R, w.V, w.AV, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true, w.oz,
+                          w.oz_bytes));
       TNX_TRY(dots(w.V, n, 1, w.AV, n, w.part, w.Hm, 1, nullptr, 0, st));
       k = 1;
       precond = 1;
@@ -439,8 +448,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       if (anchor >= max_anchor || iters >= max_iter) break;
       best = rnorm;
       best_it = iters;
-      bool reanchor = false;
-      while (!reanchor) {
+      // The bound only decides whether a converged residual is accepted; while the residual is
+      // still large the phase keeps expanding (it is then a Davidson whose row 0 is exact) and
+      // re-anchors on stagnation or once the Ritz vector has moved far from the anchor.
+      for (;;) {
         bool fell_in = false;
         TNX_TRY(expand(true, &fell_in));
         if (fell_in) break;
@@ -448,7 +459,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
           if (bound_ok()) converged = true;
           break;
         }
-        if (!bound_ok()) break;
+        if (drift + sqrt(fmax(1.0 - c0 * c0, 0.0)) > 0.3) break;
         if (rnorm < 0.9 * best) {
           best = rnorm;
           best_it = iters;

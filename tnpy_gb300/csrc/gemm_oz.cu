@@ -1,0 +1,396 @@
+// FP64-class GEMM on the tcgen05 tensor cores by exact integer slicing (Ozaki scheme).
+//
+//   C = alpha op(A) op(B) + beta C,   FP64 in and out.
+//
+// Row i of op(A) is scaled by 2^-ea_i so that its entries are below 1 in magnitude and cut, by
+// integer extraction from the 53-bit mantissa in fixed point, into S = 8 slices of 7 bits:
+//   op(A)_ik 2^-ea_i = sum_{s<S} qa_s,ik 2^-7(s+1) + r_ik,   |r_ik| < 2^-56,   |qa_s,ik| <= 127,
+// integers that BF16 holds exactly. Column j of op(B) likewise with eb_j. Then
+//   C_ij = 2^(ea_i + eb_j) sum_{g<S} 2^-7(g+2) P_g,ij + O(2^-52) per product,
+//   P_g,ij = sum_{s+t=g} sum_k qa_s,ik qb_t,kj                          (36 slice pairs),
+// and every P_g is a sum of integer products below 2^14. Over KC = 128 values of k the partial
+// sum of a group (at most 8 pairs) stays below 8 * 128 * 127^2 < 2^24, so the FP32 accumulation
+// of the tensor cores in tensor memory is exact; every KC the eight group accumulators are
+// drained into a double-FP32 running sum per output (epilogue warps), scaled by 2^-7(g+2).
+// Error: ~2^-52 per product relative to 2^ea_i 2^eb_j (the row / column maxima), plus the
+// double-FP32 summation (~2^-46 of the running sum): FP64-class where rows and columns do not
+// span many decades; at the tensor cores' rate divided by 36.
+//
+// Kernel: one 128 x 64 output tile per CTA, 6 warps: warp 0 TMA producer (all 2 S slice tiles of
+// a 32-deep K block per stage, 2 stages of 96 KB, 64-byte swizzle), warp 1 TMEM allocation (512
+// columns: eight 64-column group accumulators) and single-thread tcgen05.mma issue of the 36
+// slice products per K block, warps 2-5 epilogue. All
+// mbarrier waits are bounded (~2 s); on expiry the kernel raises the error flag and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "tc_ptx.cuh"
+#include "tnx_internal.cuh"
+
+namespace tnx {
+namespace {
+
+using namespace tc;
+
+constexpr int OZ_S = 8;                         // slices per operand
+constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;  // BK = 32 bf16 = one 64-byte swizzle row
+constexpr int OZ_KC = 128;                      // K values per exact accumulation chunk
+constexpr int OZ_STAGES = 2;                    // a stage holds all 2 S slice tiles of one K block
+constexpr int OZ_THREADS = 192;
+constexpr uint32_t OZ_TMEM_COLS = 512;
+
+// ---------------------------------------------------------------- operand slicing
+// Logical operand X(r, k) = src[r * rs + k * ks], rows x K (FP64). exps[r] = row scale exponent
+// E (|X(r, k)| < 2^E for all k; 0 for an all-zero row). One CTA (32 x 8 threads) per 32 rows.
+__global__ void oz_rowexp_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
+                                 int* __restrict__ exps, int64_t rows_pad) {
+  __shared__ int tile[32][33];
+  const int64_t r0 = int64_t(blockIdx.x) * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  int best = 0;  // biased exponent, 0 = zero / denormal
+  for (int64_t k0 = 0; k0 < K; k0 += 32) {
+    for (int i = ty; i < 32; i += 8) {
+      // unit stride along k: tx runs over k; along r: tx runs over r
+      const int64_t r = ks == 1 ? r0 + i : r0 + tx, k = ks == 1 ? k0 + tx : k0 + i;
+      int e = 0;
+      if (r < rows && k < K) e = int((unsigned(__double_as_longlong(src[r * rs + k * ks]) >> 52)) & 0x7ffu);
+      if (ks == 1) tile[i][tx] = e;
+      else tile[tx][i] = e;
+    }
+    __syncthreads();
+    if (ty == 0)
+      for (int j = 0; j < 32; ++j) best = max(best, tile[tx][j]);
+    __syncthreads();
+  }
+  if (ty == 0 && r0 + tx < rows_pad) exps[r0 + tx] = (best > 0 && r0 + tx < rows) ? best - 1022 : 0;
+}
+
+// bf16 bit pattern of an integer 0 <= q <= 127 (exact)
+__device__ __forceinline__ uint16_t bf16_of_small_int(unsigned q, unsigned sign) {
+  if (q == 0u) return 0;
+  const int e = 31 - __clz(q);
+  const unsigned mant = (q << (7 - e)) & 0x7fu;
+  return uint16_t((sign << 15) | (unsigned(127 + e) << 7) | mant);
+}
+
+// planes[s][r][k] (row pitch Kp, rows_pad rows per plane) = slice s of X(r, k) 2^-exps[r];
+// zero for r >= rows or k >= K.
+__global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
+                                const int* __restrict__ exps, uint16_t* __restrict__ planes, int64_t rows_pad,
+                                int64_t Kp) {
+  __shared__ double tile[32][33];
+  const int64_t r0 = int64_t(blockIdx.y) * 32, k0 = int64_t(blockIdx.x) * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = ks == 1 ? r0 + i : r0 + tx, k = ks == 1 ? k0 + tx : k0 + i;
+    const double v = (r < rows && k < K) ? src[r * rs + k * ks] : 0.0;
+    if (ks == 1) tile[i][tx] = v;
+    else tile[tx][i] = v;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = r0 + i, k = k0 + tx;
+    if (r >= rows_pad || k >= Kp) continue;
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(tile[i][tx]));
+    const unsigned sign = unsigned(u >> 63);
+    const int eb = int((u >> 52) & 0x7ffu);
+    unsigned long long F = 0;  // |x| 2^-E in fixed point with 63 fraction bits
+    if (eb != 0 && r < rows) {
+      const unsigned long long m53 = (u & ((1ull << 52) - 1)) | (1ull << 52);
+      const int shift = eb - 1012 - exps[r];  // <= 10 since |x| < 2^E
+      F = shift >= 0 ? (m53 << shift) : (-shift < 64 ? (m53 >> -shift) : 0ull);
+    }
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) {
+      const unsigned q = unsigned(F >> (63 - 7 * (s + 1))) & 0x7fu;
+      planes[(size_t(s) * rows_pad + r) * Kp + k] = bf16_of_small_int(q, sign);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- GEMM kernel
+// Stage layout (one K block of 32): A slices 0..S-1 (128 x 32 bf16, 8 KB each), then B slices
+// 0..S-1 (64 x 32 bf16, 4 KB each), 64-byte swizzle; every slice tile is loaded once per K
+// block and feeds all S(S+1)/2 slice products that use it.
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    oz_gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int M, int N,
+                   int Kp, int Mp, int Np, const int* __restrict__ ea, const int* __restrict__ eb, double alpha,
+                   double beta, double* __restrict__ C, int64_t ldc, int* __restrict__ err_flag) {
+  constexpr uint32_t A_TILE = OZ_BM * OZ_BK * 2, B_TILE = OZ_BN * OZ_BK * 2;
+  constexpr uint32_t STAGE_BYTES = OZ_S * (A_TILE + B_TILE);
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar[OZ_STAGES], empty_bar[OZ_STAGES], chunk_full, chunk_empty;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int abort_sh;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int m0 = blockIdx.y * OZ_BM, n0 = blockIdx.x * OZ_BN;
+  const int kblocks = Kp / OZ_BK;
+  const int kb_per_chunk = OZ_KC / OZ_BK;
+  const int nchunks = (kblocks + kb_per_chunk - 1) / kb_per_chunk;
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < OZ_STAGES; ++st) {
+      mbar_init(smem_u32(&full_bar[st]), 1);
+      mbar_init(smem_u32(&empty_bar[st]), 1);
+    }
+    mbar_init(smem_u32(&chunk_full), 1);
+    mbar_init(smem_u32(&chunk_empty), 4);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                 "r"(OZ_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer: one K block per stage
+    if (lane == 0) {
+      int issued = 0;
+      for (int kb = 0; kb < kblocks; ++kb) {
+        const int st = kb % OZ_STAGES;
+        const uint32_t ph = (kb / OZ_STAGES) & 1;
+        if (kb >= OZ_STAGES && !mbar_wait(smem_u32(&empty_bar[st]), ph ^ 1)) {
+          atomicExch(err_flag, 1);
+          abort_sh = 1;
+          break;
+        }
+        if (*((volatile int*)&abort_sh)) break;
+        const uint32_t sa = base + st * STAGE_BYTES, sb = sa + OZ_S * A_TILE;
+        const uint32_t fb = smem_u32(&full_bar[st]);
+        mbar_expect_tx(fb, STAGE_BYTES);
+        for (int q = 0; q < OZ_S; ++q) {
+          tma_load_2d(sa + q * A_TILE, &ta, fb, kb * OZ_BK, q * Mp + m0);
+          tma_load_2d(sb + q * B_TILE, &tb, fb, kb * OZ_BK, q * Np + n0);
+        }
+        ++issued;
+      }
+      for (int kb = issued - OZ_STAGES < 0 ? 0 : issued - OZ_STAGES; kb < issued; ++kb)
+        mbar_wait(smem_u32(&full_bar[kb % OZ_STAGES]), (kb / OZ_STAGES) & 1);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = instr_desc_bf16(OZ_BM, OZ_BN);
+      bool ok = true;
+      for (int c = 0; c < nchunks && ok; ++c) {
+        // the epilogue must have read the previous chunk's accumulators
+        if (c > 0 && !mbar_wait(smem_u32(&chunk_empty), (c - 1) & 1)) {
+          atomicExch(err_flag, 1);
+          abort_sh = 1;
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int kb_end = min(kblocks, (c + 1) * kb_per_chunk);
+        for (int kb = c * kb_per_chunk; kb < kb_end; ++kb) {
+          const int st = kb % OZ_STAGES;
+          const uint32_t ph = (kb / OZ_STAGES) & 1;
+          if (!mbar_wait(smem_u32(&full_bar[st]), ph) || *((volatile int*)&abort_sh)) {
+            atomicExch(err_flag, 1);
+            abort_sh = 1;
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t sa = base + st * STAGE_BYTES, sb = sa + OZ_S * A_TILE;
+          const bool chunk_start = kb == c * kb_per_chunk;
+          for (int g = 0; g < OZ_S; ++g) {
+            const uint32_t dst = tmem + uint32_t(g * OZ_BN);
+            for (int q = 0; q <= g; ++q) {  // slice pair (q, g - q)
+#pragma unroll
+              for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+                const uint64_t ad = smem_desc_sw64(sa + q * A_TILE + kk * 32);
+                const uint64_t bd = smem_desc_sw64(sb + (g - q) * B_TILE + kk * 32);
+                mma_bf16(dst, ad, bd, idesc, (chunk_start && q == 0 && kk == 0) ? 0u : 1u);
+              }
+            }
+          }
+          mma_commit(smem_u32(&empty_bar[st]));
+        }
+        if (ok) mma_commit(smem_u32(&chunk_full));
+      }
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2..5): row = lane of quad
+    const int quad = warp & 3;
+    const int row = m0 + quad * 32 + lane;
+    float hi[OZ_BN], lo[OZ_BN];
+#pragma unroll
+    for (int j = 0; j < OZ_BN; ++j) hi[j] = lo[j] = 0.f;
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+      if (!mbar_wait(smem_u32(&chunk_full), c & 1)) {
+        if (lane == 0) atomicExch(err_flag, 1);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+      for (int g = 0; g < OZ_S; ++g) {
+        const float scale = __uint_as_float(uint32_t(127 - 7 * (g + 2)) << 23);  // 2^-7(g+2)
+#pragma unroll
+        for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + uint32_t(g * OZ_BN + c0), r);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float v = __uint_as_float(r[j]) * scale;  // exact: power-of-two scaling
+            float sum, err;
+            two_sum_f(hi[c0 + j], v, sum, err);
+            hi[c0 + j] = sum;
+            lo[c0 + j] += err;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&chunk_empty)) : "memory");
+    }
+    if (ok && row < M) {
+      const int er = ea[row];
+      double* o = C + int64_t(row) * ldc + n0;
+#pragma unroll
+      for (int j = 0; j < OZ_BN; ++j) {
+        if (n0 + j < N) {
+          double v = ldexp(join_df(hi[j], lo[j]), er + eb[n0 + j]);
+          v *= alpha;
+          if (beta != 0.0) v = fma(beta, o[j], v);
+          o[j] = v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
+  }
+}
+
+struct OzLayout {
+  int64_t Mp, Np, Kp;
+  uint16_t *sa, *sb;
+  int *ea, *eb, *flag;
+};
+
+size_t oz_layout(int64_t m, int64_t n, int64_t k, void* base, OzLayout* L) {
+  OzLayout o;
+  o.Mp = (m + OZ_BM - 1) / OZ_BM * OZ_BM;
+  o.Np = (n + OZ_BN - 1) / OZ_BN * OZ_BN;
+  o.Kp = (k + OZ_BK - 1) / OZ_BK * OZ_BK;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t r = off; off += align_up(bytes); return r; };
+  const size_t osa = take(size_t(OZ_S) * o.Mp * o.Kp * 2), osb = take(size_t(OZ_S) * o.Np * o.Kp * 2),
+               oea = take(size_t(o.Mp) * 4), oeb = take(size_t(o.Np) * 4), ofl = take(4);
+  if (base && L) {
+    char* b = static_cast<char*>(base);
+    o.sa = reinterpret_cast<uint16_t*>(b + osa);
+    o.sb = reinterpret_cast<uint16_t*>(b + osb);
+    o.ea = reinterpret_cast<int*>(b + oea);
+    o.eb = reinterpret_cast<int*>(b + oeb);
+    o.flag = reinterpret_cast<int*>(b + ofl);
+    *L = o;
+  }
+  return off;
+}
+
+size_t oz_smem_bytes() { return size_t(OZ_STAGES) * OZ_S * (OZ_BM * OZ_BK * 2 + OZ_BN * OZ_BK * 2) + 1024; }
+
+}  // namespace
+
+size_t gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k) { return oz_layout(m, n, k, nullptr, nullptr); }
+
+int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+            const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws, size_t ws_bytes,
+            cudaStream_t st) {
+  if (m <= 0 || n <= 0) return TNX_OK;
+  if (k <= 0) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+  TNX_CHECK_SHAPE(m <= (int64_t(1) << 30) / OZ_S && n <= (int64_t(1) << 30) / OZ_S, "gemm_oz: operand too large");
+  OzLayout L;
+  const size_t need = oz_layout(m, n, k, ws, &L);
+  if (!ws || ws_bytes < need) {
+    set_error("gemm_oz: workspace %zu bytes < required %zu", ws_bytes, need);
+    return TNX_ERR_WORKSPACE;
+  }
+  // op(A)(i, kk): ta ? A[kk lda + i] : A[i lda + kk];  op(B) column j: tb ? B[j ldb + kk] : B[kk ldb + j]
+  const int64_t a_rs = ta ? 1 : lda, a_ks = ta ? lda : 1;
+  const int64_t b_rs = tb ? ldb : 1, b_ks = tb ? 1 : ldb;
+  dim3 tb2(32, 8);
+  oz_rowexp_kernel<<<unsigned(L.Mp / 32), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea, L.Mp);
+  TNX_LAUNCH_CHECK();
+  oz_rowexp_kernel<<<unsigned(L.Np / 32), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb, L.Np);
+  TNX_LAUNCH_CHECK();
+  oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Mp / 32)), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea, L.sa,
+                                                                                  L.Mp, L.Kp);
+  TNX_LAUNCH_CHECK();
+  oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Np / 32)), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb, L.sb,
+                                                                                  L.Np, L.Kp);
+  TNX_LAUNCH_CHECK();
+  CUtensorMap ma, mb;
+  TNX_TRY(make_tma_map_bf16(&ma, L.sa, int64_t(OZ_S) * L.Mp, L.Kp, OZ_BK, OZ_BM));
+  TNX_TRY(make_tma_map_bf16(&mb, L.sb, int64_t(OZ_S) * L.Np, L.Kp, OZ_BK, OZ_BN));
+  const size_t smem = oz_smem_bytes();
+  static std::atomic<bool> attr{false};  // idempotent setup; threads may race to it
+  if (!attr.load()) {
+    TNX_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    attr.store(true);
+  }
+  TNX_CUDA(cudaMemsetAsync(L.flag, 0, sizeof(int), st));
+  dim3 grid(unsigned(L.Np / OZ_BN), unsigned(L.Mp / OZ_BM));
+  profile_mark(KF_OZ_GEMM, st, true);
+  oz_gemm_kernel<<<grid, OZ_THREADS, smem, st>>>(ma, mb, int(m), int(n), int(L.Kp), int(L.Mp), int(L.Np), L.ea, L.eb,
+                                                 alpha, beta, C, ldc, L.flag);
+  profile_mark(KF_OZ_GEMM, st, false);
+  profile_work(KF_OZ_GEMM, 2.0 * double(m) * n * k, 8.0 * (double(m) * k + double(k) * n + double(m) * n));
+  TNX_LAUNCH_CHECK();
+  return TNX_OK;
+}
+
+int gemm_oz_flag(void* ws, int64_t m, int64_t n, int64_t k, int** flag) {
+  OzLayout L;
+  oz_layout(m, n, k, ws, &L);
+  *flag = L.flag;
+  return TNX_OK;
+}
+
+}  // namespace tnx
+
+using namespace tnx;
+
+extern "C" {
+
+size_t tnx_gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k) { return gemm_oz_workspace_bytes(m, n, k); }
+
+int tnx_gemm_oz(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+                const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* workspace,
+                size_t workspace_bytes, void* stream) {
+  TNX_CHECK_ARG(A && B && C, "null pointer");
+  TNX_CHECK_ARG(m >= 0 && n >= 0 && k >= 0, "negative size");
+  cudaStream_t st = as_stream(stream);
+  TNX_TRY(gemm_oz(trans_a != 0, trans_b != 0, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, workspace,
+                  workspace_bytes, st));
+  // a bounded wait that expired inside the kernel is reported here (one 4-byte read)
+  int* flag = nullptr;
+  gemm_oz_flag(workspace, m, n, k, &flag);
+  int h = 0;
+  TNX_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  TNX_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("tnx_gemm_oz: a bounded wait in the tensor-core kernel expired");
+    return TNX_ERR_TIMEOUT;
+  }
+  return TNX_OK;
+}
+
+}  // extern "C"

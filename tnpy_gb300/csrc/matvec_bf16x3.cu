@@ -27,99 +27,18 @@
 
 #include <atomic>
 
+#include "tc_ptx.cuh"
 #include "tnx_internal.cuh"
 
 namespace tnx {
 namespace {
 
+using namespace tc;
+
 constexpr int BM = 128;
 constexpr int BK = 64;  // 64 bf16 = 128 bytes = one swizzle atom row
 constexpr int STAGES = 4;
 constexpr int GEMM_THREADS = 192;
-constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-
-// ---------------------------------------------------------------- PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait: true when the phase completed, false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > WAIT_CYCLES) return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
-      : "memory");
-}
-
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
-  // K-major operand, 128-byte swizzle: 8-row groups 1024 bytes apart (SBO), LBO unused,
-  // descriptor version 1 (bits 46-47), layout type 2 = SWIZZLE_128B (bits 61-63)
-  uint64_t d = 0;
-  d |= uint64_t((addr >> 4) & 0x3FFF);
-  d |= uint64_t(1) << 16;                // LBO (ignored for swizzled K-major)
-  d |= uint64_t(1024 >> 4) << 32;        // SBO
-  d |= uint64_t(1) << 46;                // version
-  d |= uint64_t(2) << 61;                // SWIZZLE_128B
-  return d;
-}
-
-__host__ __device__ constexpr uint32_t instr_desc_bf16(int m, int n) {
-  // D = F32 (bits 4-5 = 1), A = BF16 (bits 7-9 = 1), B = BF16 (bits 10-12 = 1), both K-major,
-  // N >> 3 at bits 17-22, M >> 4 at bits 24-28
-  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 // ---------------------------------------------------------------- GEMM kernel
 // C[M, N] = sum_k A[m, k] B[n, k] over the three split products; A*, B* are K-major BF16
@@ -333,46 +252,9 @@ __global__ void zero_pad_kernel(__nv_bfloat16* __restrict__ hi, __nv_bfloat16* _
 }
 
 // ---------------------------------------------------------------- host side
-using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeFn get_encode() {
-  static EncodeFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeFn>(p);
-  }
-  return fn;
-}
-
 // 2-D map over a K-major bf16 matrix rows x ldp (K innermost), box {64, box_rows}, 128B swizzle
 int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t ldp, int box_rows) {
-  EncodeFn enc = get_encode();
-  if (!enc) {
-    set_error("cuTensorMapEncodeTiled unavailable");
-    return TNX_ERR_CUDA;
-  }
-  if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0 || (ldp * 2) % 16 != 0) {
-    set_error("TMA operand misaligned");
-    return TNX_ERR_INVALID_ARG;
-  }
-  cuuint64_t dims[2] = {cuuint64_t(ldp), cuuint64_t(rows)};
-  cuuint64_t strides[1] = {cuuint64_t(ldp * 2)};
-  cuuint32_t box[2] = {cuuint32_t(BK), cuuint32_t(box_rows)};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    set_error("cuTensorMapEncodeTiled failed (%d)", int(r));
-    return TNX_ERR_CUDA;
-  }
-  return TNX_OK;
+  return make_tma_map_bf16(map, ptr, rows, ldp, BK, box_rows);
 }
 
 template <int BN>
@@ -455,6 +337,47 @@ dim3 tgrid(int64_t rows, int64_t cols) {
 }
 
 }  // namespace
+
+using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeFn get_encode() {
+  static EncodeFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      return reinterpret_cast<EncodeFn>(p);
+    return static_cast<EncodeFn>(nullptr);
+  }();
+  return fn;
+}
+
+int make_tma_map_bf16(CUtensorMap* map, const void* ptr, int64_t rows, int64_t ldp, int box_k, int box_rows) {
+  EncodeFn enc = get_encode();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled unavailable");
+    return TNX_ERR_CUDA;
+  }
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0 || (ldp * 2) % 16 != 0 || (box_k != 64 && box_k != 32)) {
+    set_error("TMA operand misaligned");
+    return TNX_ERR_INVALID_ARG;
+  }
+  cuuint64_t dims[2] = {cuuint64_t(ldp), cuuint64_t(rows)};
+  cuuint64_t strides[1] = {cuuint64_t(ldp * 2)};
+  cuuint32_t box[2] = {cuuint32_t(box_k), cuuint32_t(box_rows)};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", int(r));
+    return TNX_ERR_CUDA;
+  }
+  return TNX_OK;
+}
 
 bool mixed_supported(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr) {
   return chi_l >= 16 && chi_r >= 16 && dl * d <= 64 && dr * d <= 64 && dl * chi_l < (1 << 30);

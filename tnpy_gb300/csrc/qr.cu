@@ -369,238 +369,6 @@ __global__ void __launch_bounds__(PT) panel_cl_kernel(double* __restrict__ F, in
   cluster_wait_acquire();
 }
 
-// Double-FP32 form of panel_cl_kernel for the gauge move's FP64-class precision modes: the
-// same steps, exchange and T recurrence, with the panel, v and the next column held in shared
-// memory as (hi, lo) float planes and the per-element updates and dot products done in
-// double-FP32 arithmetic on the FP32 pipe (~2^-46 per operation) instead of the FP64 pipe,
-// which on this part issues ~2 FMA/clock/SM. Exchanged partial sums, the column scalars and T
-// stay FP64.
-template <int NB, int CL>
-__global__ void __launch_bounds__(PT) panel_cl_df_kernel(double* __restrict__ F, int64_t m, int64_t j0, int nb,
-                                                         int ld, double* __restrict__ tau_out,
-                                                         double* __restrict__ T_out) {
-  constexpr int TPC = PT / NB;
-  cg::cluster_group cluster = cg::this_cluster();
-  const int q = int(cluster.block_rank());
-  extern __shared__ float plf[];     // hi plane [NB][ld], lo plane [NB][ld], then v and next column
-  float* ph = plf;
-  float* pw = plf + NB * ld;         // lo plane
-  float* vh = pw + NB * ld;
-  float* vl = vh + ld;
-  float* nh = vl + ld;
-  float* nl = nh + ld;
-  __shared__ double slot[2][3 * NB];
-  __shared__ double S[NB], P[NB], Z[NB], taus[NB], sc[4];
-  __shared__ double Ts[NB][NB + 1];
-  const int tid = threadIdx.x, ci = tid / TPC, h = tid % TPC;
-  const int64_t mp = m - j0;
-  const int64_t rpc = (mp + CL - 1) / CL;
-  const int64_t r0 = int64_t(q) * rpc;
-  const int rows = int(r0 >= mp ? 0 : (mp - r0 < rpc ? mp - r0 : rpc));
-  for (int e = tid; e < nb * rows; e += PT) {
-    const int c = e / rows, r = e % rows;
-    split_df(F[(j0 + c) * m + j0 + r0 + r], ph[c * ld + r], pw[c * ld + r]);
-  }
-  __syncthreads();
-  {
-    float ah = 0.f, al = 0.f;
-    if (ci < nb) {
-      const int rs = r0 > 0 ? 0 : 1;
-      for (int i = rs / TPC; i * TPC < rows; ++i) {
-        const int r = i * TPC + h;
-        if (r >= rs && r < rows) df_fma_acc(ph[r], pw[r], ph[ci * ld + r], pw[ci * ld + r], ah, al);
-      }
-    }
-    double acc = join_df(ah, al);
-#pragma unroll
-    for (int o = TPC / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (ci < nb && h == 0) {
-      slot[0][ci] = acc;
-      if (r0 == 0 && rows > 0) slot[0][NB + ci] = join_df(ph[ci * ld], pw[ci * ld]);
-    }
-  }
-  cluster_arrive_release();
-  cluster_wait_acquire();
-  for (int jj = 0; jj < nb; ++jj) {
-    const int par = jj & 1;
-    const int owner = int(jj / rpc);
-    if (tid < NB) {
-      const int c = tid;
-      if (c >= jj && c < nb) {
-        double t = 0.0;
-#pragma unroll
-        for (int qq = 0; qq < CL; ++qq) t += cluster.map_shared_rank(&slot[par][0], qq)[c];
-        S[c] = t;
-        P[c] = cluster.map_shared_rank(&slot[par][NB], owner)[c];
-      }
-    } else if (tid < 2 * NB && q == 0) {
-      const int a = tid - NB;
-      if (a < jj - 1) {
-        double t = 0.0;
-#pragma unroll
-        for (int qq = 0; qq < CL; ++qq) t += cluster.map_shared_rank(&slot[par][2 * NB], qq)[a];
-        Z[a] = t;
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      const double sigma = S[jj], alpha = P[jj];
-      double tj = 0.0, beta = alpha, scale = 0.0;
-      if (sigma != 0.0) {
-        const double nrm = sqrt(alpha * alpha + sigma);
-        beta = alpha >= 0.0 ? -nrm : nrm;
-        tj = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-      }
-      sc[0] = tj;
-      sc[1] = beta;
-      sc[2] = scale;
-      sc[3] = jj + 1 < nb ? tj * (P[jj + 1] + scale * S[jj + 1]) : 0.0;
-      taus[jj] = tj;
-    }
-    __syncthreads();
-    const double tj = sc[0], beta = sc[1];
-    float sch, scl, wnh, wnl;
-    split_df(sc[2], sch, scl);
-    split_df(sc[3], wnh, wnl);
-    const bool has_next = jj + 1 < nb;
-    double* nxt = slot[par ^ 1];
-    float* xjh = ph + jj * ld;
-    float* xjl = pw + jj * ld;
-    float* xnh = ph + (jj + 1) * ld;
-    float* xnl = pw + (jj + 1) * ld;
-    const int64_t lj = jj - r0;
-    // ---- phase A
-    for (int r = int(lj > 0 ? lj : 0) + tid; r < rows; r += PT) {
-      float a, b;
-      if (r == lj) {
-        a = 1.f;
-        b = 0.f;
-      } else {
-        df_mul(sch, scl, xjh[r], xjl[r], a, b);
-      }
-      vh[r] = a;
-      vl[r] = b;
-      if (has_next) df_fms(xnh[r], xnl[r], wnh, wnl, a, b, nh[r], nl[r]);
-    }
-    __syncthreads();
-    // ---- phase B
-    float ah = 0.f, al = 0.f;
-    if (ci < nb && ci != jj) {
-      float* xch = ph + ci * ld;
-      float* xcl = pw + ci * ld;
-      const int64_t ln = lj + 1;
-      const bool own_ln = ln >= 0 && ln < rows && ln % TPC == h;
-      if (ci == jj + 1) {
-        if (own_ln) nxt[NB + ci] = join_df(nh[ln], nl[ln]);
-        const int rs = int(lj + 2 > 0 ? lj + 2 : 0);
-        for (int i = rs / TPC; i * TPC < rows; ++i) {
-          const int r = i * TPC + h;
-          if (r >= rs && r < rows) df_fma_acc(nh[r], nl[r], nh[r], nl[r], ah, al);
-        }
-      } else if (ci > jj) {
-        float wch, wcl;
-        split_df(tj * (P[ci] + sc[2] * S[ci]), wch, wcl);
-        if (lj >= 0 && lj < rows && lj % TPC == h)  // v_jj[jj] = 1
-          df_fms(xch[lj], xcl[lj], wch, wcl, 1.f, 0.f, xch[lj], xcl[lj]);
-        if (own_ln) {
-          df_fms(xch[ln], xcl[ln], wch, wcl, vh[ln], vl[ln], xch[ln], xcl[ln]);
-          nxt[NB + ci] = join_df(xch[ln], xcl[ln]);
-        }
-        const int rs = int(lj + 2 > 0 ? lj + 2 : 0);
-        for (int i = rs / TPC; i * TPC < rows; ++i) {
-          const int r = i * TPC + h;
-          if (r < rs || r >= rows) continue;
-          float a, b;
-          df_fms(xch[r], xcl[r], wch, wcl, vh[r], vl[r], a, b);
-          xch[r] = a;
-          xcl[r] = b;
-          df_fma_acc(nh[r], nl[r], a, b, ah, al);
-        }
-      } else {
-        const int rs = int(lj > 0 ? lj : 0);
-        for (int i = rs / TPC; i * TPC < rows; ++i) {
-          const int r = i * TPC + h;
-          if (r >= rs && r < rows) df_fma_acc(xch[r], xcl[r], vh[r], vl[r], ah, al);
-        }
-      }
-    }
-    double acc = join_df(ah, al);
-#pragma unroll
-    for (int o = TPC / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (ci < nb && ci != jj && h == 0) {
-      if (ci > jj) nxt[ci] = acc;
-      else nxt[2 * NB + ci] = acc;
-    }
-    cluster_arrive_release();
-    __syncthreads();
-    // ---- phase C
-    {
-      float bh, bl;
-      split_df(beta, bh, bl);
-      for (int r = int(lj > 0 ? lj : 0) + tid; r < rows; r += PT) {
-        if (r == lj) {
-          xjh[r] = bh;
-          xjl[r] = bl;
-        } else {
-          xjh[r] = vh[r];
-          xjl[r] = vl[r];
-        }
-        if (has_next) {
-          xnh[r] = nh[r];
-          xnl[r] = nl[r];
-        }
-      }
-      if (q == 0 && jj >= 1 && tid < jj) {
-        const int k = jj - 1, a = tid;
-        if (a == k) {
-          Ts[k][k] = taus[k];
-        } else {
-          double t = 0.0;
-          for (int c = a; c < k; ++c) t = fma(Ts[a][c], Z[c], t);
-          Ts[a][k] = -taus[k] * t;
-        }
-      }
-    }
-    __syncthreads();
-    cluster_wait_acquire();
-  }
-  if (q == 0 && tid >= NB && tid < 2 * NB) {
-    const int a = tid - NB;
-    if (a < nb - 1) {
-      double t = 0.0;
-#pragma unroll
-      for (int qq = 0; qq < CL; ++qq) t += cluster.map_shared_rank(&slot[nb & 1][2 * NB], qq)[a];
-      Z[a] = t;
-    }
-  }
-  __syncthreads();
-  if (q == 0 && tid < nb) {
-    const int k = nb - 1, a = tid;
-    if (a == k) {
-      Ts[k][k] = taus[k];
-    } else {
-      double t = 0.0;
-      for (int c = a; c < k; ++c) t = fma(Ts[a][c], Z[c], t);
-      Ts[a][k] = -taus[k] * t;
-    }
-  }
-  __syncthreads();
-  if (q == 0) {
-    for (int e = tid; e < NB * NB; e += PT) {
-      const int b = e / NB, a = e % NB;
-      T_out[e] = (a <= b && b < nb) ? Ts[a][b] : 0.0;
-    }
-    for (int b = tid; b < NB; b += PT) tau_out[b] = b < nb ? taus[b] : 0.0;
-  }
-  for (int e = tid; e < nb * rows; e += PT) {
-    const int c = e / rows, r = e % rows;
-    F[(j0 + c) * m + j0 + r0 + r] = join_df(ph[c * ld + r], pw[c * ld + r]);
-  }
-  cluster_arrive_release();
-  cluster_wait_acquire();
-}
-
 // dst (row-major rows x cols) <-> col-major transposed copy
 __global__ void transpose_kernel(const double* __restrict__ src, int64_t rows, int64_t cols,
                                  double* __restrict__ dst) {
@@ -699,18 +467,12 @@ struct PanelKernelInfo {
   size_t max_dyn = 0;
 };
 
-template <int NB, int CL, bool DF>
-constexpr auto panel_kernel_ptr() {
-  if constexpr (DF) return panel_cl_df_kernel<NB, CL>;
-  else return panel_cl_kernel<NB, CL>;
-}
-
-template <int NB, int CL, bool DF>
+template <int NB, int CL>
 const PanelKernelInfo& panel_info() {
   static PanelKernelInfo info;
   static std::once_flag once;
   std::call_once(once, [] {
-    auto k = panel_kernel_ptr<NB, CL, DF>();
+    auto k = panel_cl_kernel<NB, CL>;
     cudaFuncAttributes fa{};
     int dev = 0, optin = 0;
     if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
@@ -746,7 +508,7 @@ const PanelKernelInfo& panel_info() {
   return info;
 }
 
-template <int NB, int CL, bool DF>
+template <int NB, int CL>
 int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* T, cudaStream_t st) {
   const int64_t rpc = (m - j0 + CL - 1) / CL;
   const int ld = panel_ld(rpc, PT / NB);
@@ -762,7 +524,7 @@ int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* 
   cfg.stream = st;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  TNX_CUDA(cudaLaunchKernelEx(&cfg, panel_kernel_ptr<NB, CL, DF>(), F, m, j0, nb, ld, tau, T));
+  TNX_CUDA(cudaLaunchKernelEx(&cfg, panel_cl_kernel<NB, CL>, F, m, j0, nb, ld, tau, T));
   TNX_LAUNCH_CHECK();
   return TNX_OK;
 }
@@ -772,36 +534,28 @@ int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* 
 // GEMMs a longer K; 16-CTA clusters (where the device schedules them) spread the panel's FP64
 // arithmetic over twice the SMs of the portable 8.
 // TNX_QR_CLUSTER=8 or 16 restricts the cluster size (tuning).
-// The double-FP32 kernel (df) serves the FP64-class precision modes whose trailing updates are
-// double-FP32 GEMMs as well; the FP64 mode keeps the FP64 kernel.
 struct PanelPlan {
   int nb, cl;
-  bool df;
 };
 
-template <int NB, int CL, bool DF>
+template <int NB, int CL>
 bool panel_fits(int64_t m) {
-  const PanelKernelInfo& info = panel_info<NB, CL, DF>();
+  const PanelKernelInfo& info = panel_info<NB, CL>();
   const int64_t rpc = (m + CL - 1) / CL;
   return info.ok && size_t(NB + 2) * panel_ld(rpc, PT / NB) * sizeof(double) <= info.max_dyn;
 }
 
-template <bool DF>
-PanelPlan plan_panels_t(int64_t m, int only) {
-  const bool c8 = only == 0 || only == 8, c16 = only == 0 || only == 16;
-  if (c16 && panel_fits<64, 16, DF>(m)) return {64, 16, DF};
-  if (c8 && panel_fits<64, 8, DF>(m)) return {64, 8, DF};
-  if (c16 && panel_fits<32, 16, DF>(m)) return {32, 16, DF};
-  if (c8 && panel_fits<32, 8, DF>(m)) return {32, 8, DF};
-  return {QB, 0, false};
-}
-
-PanelPlan plan_panels(int64_t m, bool df) {
+PanelPlan plan_panels(int64_t m) {
   static const int only = [] {
     const char* e = getenv("TNX_QR_CLUSTER");
     return e ? atoi(e) : 0;
   }();
-  return df ? plan_panels_t<true>(m, only) : plan_panels_t<false>(m, only);
+  const bool c8 = only == 0 || only == 8, c16 = only == 0 || only == 16;
+  if (c16 && panel_fits<64, 16>(m)) return {64, 16};
+  if (c8 && panel_fits<64, 8>(m)) return {64, 8};
+  if (c16 && panel_fits<32, 16>(m)) return {32, 16};
+  if (c8 && panel_fits<32, 8>(m)) return {32, 8};
+  return {QB, 0};
 }
 
 int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, double* tau, double* T,
@@ -811,16 +565,10 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
   if (pp.cl == 0) {
     panel_kernel<<<1, QT, 0, st>>>(F, m, j0, nb, tau, T);
     TNX_LAUNCH_CHECK();
-  } else if (pp.df) {
-    if (pp.nb == 64) rc = pp.cl == 16 ? launch_panel<64, 16, true>(F, m, j0, nb, tau, T, st)
-                                      : launch_panel<64, 8, true>(F, m, j0, nb, tau, T, st);
-    else rc = pp.cl == 16 ? launch_panel<32, 16, true>(F, m, j0, nb, tau, T, st)
-                          : launch_panel<32, 8, true>(F, m, j0, nb, tau, T, st);
+  } else if (pp.nb == 64) {
+    rc = pp.cl == 16 ? launch_panel<64, 16>(F, m, j0, nb, tau, T, st) : launch_panel<64, 8>(F, m, j0, nb, tau, T, st);
   } else {
-    if (pp.nb == 64) rc = pp.cl == 16 ? launch_panel<64, 16, false>(F, m, j0, nb, tau, T, st)
-                                      : launch_panel<64, 8, false>(F, m, j0, nb, tau, T, st);
-    else rc = pp.cl == 16 ? launch_panel<32, 16, false>(F, m, j0, nb, tau, T, st)
-                          : launch_panel<32, 8, false>(F, m, j0, nb, tau, T, st);
+    rc = pp.cl == 16 ? launch_panel<32, 16>(F, m, j0, nb, tau, T, st) : launch_panel<32, 8>(F, m, j0, nb, tau, T, st);
   }
   profile_mark(KF_QR_PANEL, st, false);
   return rc;
@@ -830,7 +578,7 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
 
 // Factor the column-major m x n matrix in w.F (m >= n) and form Q (column-major) in w.Qc.
 int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false) {
-  const PanelPlan pp = plan_panels(m, df);
+  const PanelPlan pp = plan_panels(m);
   const int NB = pp.nb;
   const int64_t np = (n + NB - 1) / NB;
   for (int64_t p = 0; p < np; ++p) {
@@ -907,12 +655,20 @@ int tnx_qr(const double* M, int64_t m, int64_t n, double* Q, double* R, void* wo
   return TNX_OK;
 }
 
+// slices of the R * neighbour product on the tensor cores (FP64-class modes)
+static size_t gauge_oz_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r, int64_t chi_other) {
+  const int64_t n = direction == 1 ? chi_r : chi_l;
+  const int64_t gm = direction == 1 ? n : chi_other * d, gn = direction == 1 ? d * chi_other : n;
+  return use_oz(gm, gn, n) ? gemm_oz_workspace_bytes(gm, gn, n) : 0;
+}
+
 size_t tnx_gauge_move_workspace_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r,
                                       int64_t chi_other) {
   int64_t m = direction == 1 ? chi_l * d : d * chi_r;
   int64_t n = direction == 1 ? chi_r : chi_l;
   int64_t nb_elems = direction == 1 ? chi_r * d * chi_other : chi_other * d * chi_l;
-  return qr_layout(m, n, nullptr, nullptr) + align_up(n * n * 8) + align_up(nb_elems * 8);
+  return qr_layout(m, n, nullptr, nullptr) + align_up(n * n * 8) + align_up(nb_elems * 8) +
+         align_up(gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other));
 }
 
 int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, int64_t d, int64_t chi_r,
@@ -935,6 +691,9 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
   size_t qbytes = qr_layout(m, n, workspace, &w);
   double* Rb = reinterpret_cast<double*>(static_cast<char*>(workspace) + qbytes);
   double* tmp = reinterpret_cast<double*>(static_cast<char*>(workspace) + qbytes + align_up(n * n * 8));
+  const int64_t nb_elems = direction == 1 ? chi_r * d * chi_other : chi_other * d * chi_l;
+  const size_t ozb = df ? gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other) : 0;
+  void* oz = ozb ? static_cast<void*>(reinterpret_cast<char*>(tmp) + align_up(nb_elems * 8)) : nullptr;
   cudaStream_t st = as_stream(stream);
   dim3 tb(32, 8);
   if (direction == 1) {
@@ -948,7 +707,7 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
     TNX_LAUNCH_CHECK();
     // A_next (chi_r x d chi_other) <- R A_next
     const int64_t nc = d * chi_other;
-    TNX_TRY(gemm_fp64_class(df, false, false, n, nc, n, 1.0, Rb, n, 0, A_nb, nc, 0, 0.0, tmp, nc, 0, 1, st));
+    TNX_TRY(gemm_fp64_class_oz(df, false, false, n, nc, n, 1.0, Rb, n, A_nb, nc, 0.0, tmp, nc, oz, ozb, st));
     TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, n * nc * 8, cudaMemcpyDeviceToDevice, st));
   } else {
     // psi (chi_l x d chi_r) row-major == psi^T (d chi_r x chi_l) column-major
@@ -960,7 +719,7 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
     TNX_LAUNCH_CHECK();
     // A_prev (chi_other d x chi_l) <- A_prev R^T
     const int64_t mr = chi_other * d;
-    TNX_TRY(gemm_fp64_class(df, false, true, mr, n, n, 1.0, A_nb, n, 0, Rb, n, 0, 0.0, tmp, n, 0, 1, st));
+    TNX_TRY(gemm_fp64_class_oz(df, false, true, mr, n, n, 1.0, A_nb, n, Rb, n, 0.0, tmp, n, oz, ozb, st));
     TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, mr * n * 8, cudaMemcpyDeviceToDevice, st));
   }
   return TNX_OK;

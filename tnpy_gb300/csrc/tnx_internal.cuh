@@ -49,7 +49,7 @@ void count_launch();
 
 // Optional CUDA-event timing of one kernel family (enabled by tnx_profile_begin).
 enum KernelFamily { KF_TC_GEMM = 0, KF_F64_GEMM = 1, KF_VECTOR = 2, KF_QR_PANEL = 3, KF_EIGH = 4, KF_OTHER = 5,
-                    KF_COUNT = 6 };
+                    KF_OZ_GEMM = 6, KF_COUNT = 7 };
 bool profiling(int family);
 void profile_mark(int family, cudaStream_t st, bool start);
 // algorithmic work (flops, bytes) of the launch just marked, summed while profiling
@@ -127,42 +127,6 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
   e = (a - (s - bb)) + (b - bb);
 }
 
-// (rh, rl) = (xh, xl) - (wh, wl) * (vh, vl), renormalised (|rl| <= ulp(rh) / 2)
-__device__ __forceinline__ void df_fms(float xh, float xl, float wh, float wl, float vh, float vl, float& rh,
-                                       float& rl) {
-  const float p = wh * vh;
-  float pe = fmaf(wh, vh, -p);
-  pe = fmaf(wh, vl, pe);
-  pe = fmaf(wl, vh, pe);
-  float s, e;
-  two_sum_f(xh, -p, s, e);
-  e += xl - pe;
-  rh = s + e;
-  rl = e - (rh - s);
-}
-
-// (rh, rl) = (ah, al) * (bh, bl), renormalised
-__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& rh, float& rl) {
-  const float p = ah * bh;
-  float e = fmaf(ah, bh, -p);
-  e = fmaf(ah, bl, e);
-  e = fmaf(al, bh, e);
-  rh = p + e;
-  rl = e - (rh - p);
-}
-
-// (ch, cl) += (ah, al) * (bh, bl), cl left unnormalised (accumulators of long sums)
-__device__ __forceinline__ void df_fma_acc(float ah, float al, float bh, float bl, float& ch, float& cl) {
-  const float p = ah * bh;
-  float e = fmaf(ah, bh, -p);
-  e = fmaf(ah, bl, e);
-  e = fmaf(al, bh, e);
-  float s, err;
-  two_sum_f(ch, p, s, err);
-  ch = s;
-  cl += err + e;
-}
-
 // ---- FP64 GEMM (row-major, optional transposes, strided batch) --------------------
 // k_total > 0 selects split-K: batch z multiplies the K slice [z*k, min((z+1)*k, k_total))
 int gemm_f64(bool trans_a, bool trans_b, int64_t m, int64_t n, int64_t k, double alpha,
@@ -178,6 +142,12 @@ int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double al
 int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
               int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C, int64_t ldc, int64_t sc,
               int64_t batch, cudaStream_t st, int64_t k_total = 0);
+// FP64-class GEMM on the tensor cores (Ozaki slicing, gemm_oz.cu); workspace sized by
+// gemm_oz_workspace_bytes(m, n, k)
+size_t gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k);
+int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+            const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws, size_t ws_bytes,
+            cudaStream_t st);
 // df = true: double-FP32 emulation; false: native FP64
 int gemm_fp64_class(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                     int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C,
@@ -193,9 +163,17 @@ int wcontract_right(const double* T1, const double* W, double* T2, int64_t chi_l
 
 // One FP64 one-site matvec with explicit scratch (T1, T2 of matvec1_scratch_elems each).
 int64_t matvec1_scratch_elems(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr);
+// df: FP64-class (double-FP32, or the tensor-core Ozaki GEMM for large products when oz_ws
+// holds matvec1_oz_bytes); otherwise native FP64
 int matvec1_f64(const double* L, const double* W, const double* R, const double* x, double* y,
                 int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double* T1,
-                double* T2, cudaStream_t st, bool df = false);
+                double* T2, cudaStream_t st, bool df = false, void* oz_ws = nullptr, size_t oz_bytes = 0);
+size_t matvec1_oz_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr);
+bool use_oz(int64_t m, int64_t n, int64_t k);
+// gemm_fp64_class with the tensor-core FP64-class GEMM for large df products (needs oz_ws)
+int gemm_fp64_class_oz(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                       int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* oz_ws,
+                       size_t oz_bytes, cudaStream_t st);
 // FP64-class contraction selected by a precision code: TNX_FP64 -> native FP64,
 // TNX_BF16X3 / TNX_DF64 -> double-FP32 emulation
 inline bool use_df64(int precision) { return precision == TNX_BF16X3 || precision == TNX_DF64; }

@@ -227,3 +227,16 @@ def gemm_df64(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False):
     check("tnx_gemm_df64", lib.tnx_gemm_df64(int(trans_a), int(trans_b), m, n, k, 1.0, ptr(a), a.shape[1], ptr(b),
                                              b.shape[1], 0.0, ptr(out), n, stream_ptr()))
     return out
+
+
+def gemm_oz(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False):
+    """C = op(A) op(B), FP64 in / out, on the tensor cores by exact integer slicing (Ozaki)."""
+    a, b = _f64(a, "a"), _f64(b, "b")
+    m = a.shape[1] if trans_a else a.shape[0]
+    k = a.shape[0] if trans_a else a.shape[1]
+    n = b.shape[0] if trans_b else b.shape[1]
+    out = torch.empty((m, n), dtype=torch.float64, device=a.device)
+    wp, wn = Workspace.get(lib.tnx_gemm_oz_workspace_bytes(m, n, k), a.device)
+    check("tnx_gemm_oz", lib.tnx_gemm_oz(int(trans_a), int(trans_b), m, n, k, 1.0, ptr(a), a.shape[1], ptr(b),
+                                         b.shape[1], 0.0, ptr(out), n, wp, wn, stream_ptr()))
+    return out

@@ -21,7 +21,7 @@ import torch
 from . import kernels as K
 from ._lib import lib
 
-FAMILIES = ["tcgen05 GEMM", "FP64-class GEMM", "vector", "QR panel", "eigh", "other"]
+FAMILIES = ["tcgen05 GEMM", "FP64-class GEMM", "vector", "QR panel", "eigh", "other", "Ozaki GEMM"]
 
 
 def _families(fn, reps):
