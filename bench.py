@@ -368,9 +368,12 @@ def run_ours(a):
     achieved = flops.value / (tot_ms.value / 1e3) / 1e12 if tot_ms.value > 0 else None
     peak = bf16_sust / 3.0
     traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
+    tf = ROOT / "profiles" / "traffic.txt"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get(f"tc_gemm_chi{a.chi}")
+        for ln in tf.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) == 2 and not ln.startswith("#") and parts[0] == f"tc_gemm_chi{a.chi}":
+                traffic = float(parts[1])
     roofline = {"kernel": "bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)",
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "tnx_internal.cuh"
 
@@ -43,8 +44,10 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 // pass kept at least half of |t|^2: the DGKS criterion for a second classical Gram-Schmidt pass.
 __device__ __forceinline__ bool gs_pass_skipped(const double* gate) { return gate && gate[1] >= 0.5 * gate[0]; }
 
-__global__ void __launch_bounds__(DT) dots_kernel(const double* __restrict__ V, int64_t ldv,
-                                                 const double* __restrict__ w, int64_t n,
+// T = double (FP64 arithmetic) or float (FP32 products and per-thread sums, FP64 block sums)
+template <typename T>
+__global__ void __launch_bounds__(DT) dots_kernel(const T* __restrict__ V, int64_t ldv,
+                                                 const T* __restrict__ w, int64_t n,
                                                  double* __restrict__ part, int nchunk,
                                                  const double* __restrict__ gate) {
   __shared__ double sh[DT / 32];
@@ -53,8 +56,8 @@ __global__ void __launch_bounds__(DT) dots_kernel(const double* __restrict__ V, 
     if (threadIdx.x == 0) part[j * nchunk + chunk] = 0.0;
     return;
   }
-  const double* v = V + int64_t(j) * ldv;
-  double acc0 = 0.0, acc1 = 0.0;
+  const T* v = V + int64_t(j) * ldv;
+  T acc0 = T(0), acc1 = T(0);
   const int64_t stride = int64_t(nchunk) * DT;
   int64_t i = int64_t(chunk) * DT + threadIdx.x;
   for (; i + stride < n; i += 2 * stride) {
@@ -62,7 +65,7 @@ __global__ void __launch_bounds__(DT) dots_kernel(const double* __restrict__ V, 
     acc1 = fma(v[i + stride], w[i + stride], acc1);
   }
   if (i < n) acc0 = fma(v[i], w[i], acc0);
-  const double acc = block_sum(acc0 + acc1, sh);
+  const double acc = block_sum(double(acc0) + double(acc1), sh);
   if (threadIdx.x == 0) part[j * nchunk + chunk] = acc;
 }
 
@@ -83,23 +86,24 @@ __global__ void __launch_bounds__(DT) reduce_kernel(const double* __restrict__ p
 }
 
 // w -= sum_{j<k} h[j] V[j]; partial ||w||^2 (a skipped gated pass only recomputes the norm)
-__global__ void __launch_bounds__(DT) update_kernel(const double* __restrict__ V, int64_t ldv, int k,
-                                                   const double* __restrict__ h, double* __restrict__ w,
+template <typename T>
+__global__ void __launch_bounds__(DT) update_kernel(const T* __restrict__ V, int64_t ldv, int k,
+                                                   const double* __restrict__ h, T* __restrict__ w,
                                                    int64_t n, double* __restrict__ part, int nchunk,
                                                    const double* __restrict__ gate) {
   __shared__ double sh[DT / 32];
-  __shared__ double hs[MAXB];
+  __shared__ T hs[MAXB];
   const bool skip = gs_pass_skipped(gate);
-  if (threadIdx.x < k) hs[threadIdx.x] = h[threadIdx.x];
+  if (threadIdx.x < k) hs[threadIdx.x] = T(h[threadIdx.x]);
   __syncthreads();
-  double nrm = 0.0;
+  T nrm = T(0);
   for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
-    double acc = w[i];
+    T acc = w[i];
     if (!skip) {
       int j = 0;
       for (; j + 4 <= k; j += 4) {
-        const double v0 = V[int64_t(j) * ldv + i], v1 = V[int64_t(j + 1) * ldv + i];
-        const double v2 = V[int64_t(j + 2) * ldv + i], v3 = V[int64_t(j + 3) * ldv + i];
+        const T v0 = V[int64_t(j) * ldv + i], v1 = V[int64_t(j + 1) * ldv + i];
+        const T v2 = V[int64_t(j + 2) * ldv + i], v3 = V[int64_t(j + 3) * ldv + i];
         acc = fma(-hs[j], v0, acc);
         acc = fma(-hs[j + 1], v1, acc);
         acc = fma(-hs[j + 2], v2, acc);
@@ -110,38 +114,47 @@ __global__ void __launch_bounds__(DT) update_kernel(const double* __restrict__ V
     }
     nrm = fma(acc, acc, nrm);
   }
-  nrm = block_sum(nrm, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = nrm;
+  const double tot = block_sum(double(nrm), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
 // w *= 1/sqrt(nrm2[0])
-__global__ void scale_kernel(double* __restrict__ w, int64_t n, const double* __restrict__ nrm2) {
-  const double s = 1.0 / sqrt(nrm2[0]);
+template <typename T>
+__global__ void scale_kernel(T* __restrict__ w, int64_t n, const double* __restrict__ nrm2) {
+  const T s = T(1.0 / sqrt(nrm2[0]));
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
     w[i] *= s;
 }
 
+// out = T(in) (precision change of one vector)
+template <typename Tin, typename Tout>
+__global__ void convert_kernel(const Tin* __restrict__ in, Tout* __restrict__ out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = Tout(in[i]);
+}
+
 // x = V s, ax = AV s, r = ax - theta x, t = r / (diag - theta) (or r), partial ||r||^2
-__global__ void __launch_bounds__(DT) ritz_kernel(const double* __restrict__ V, const double* __restrict__ AV,
+template <typename T>
+__global__ void __launch_bounds__(DT) ritz_kernel(const T* __restrict__ V, const T* __restrict__ AV,
                                                  int64_t ldv, int k, const double* __restrict__ s,
                                                  const double* __restrict__ theta_p,
-                                                 const double* __restrict__ diag, int precond,
-                                                 double* __restrict__ x, double* __restrict__ ax,
-                                                 double* __restrict__ t, int64_t n,
+                                                 const T* __restrict__ diag, int precond,
+                                                 T* __restrict__ x, T* __restrict__ ax,
+                                                 T* __restrict__ t, int64_t n,
                                                  double* __restrict__ part, int nchunk) {
   __shared__ double sh[DT / 32];
-  __shared__ double ss[MAXB];
-  if (threadIdx.x < k) ss[threadIdx.x] = s[threadIdx.x];
+  __shared__ T ss[MAXB];
+  if (threadIdx.x < k) ss[threadIdx.x] = T(s[threadIdx.x]);
   __syncthreads();
-  const double theta = theta_p[0];
-  double nrm = 0.0;
+  const T theta = T(theta_p[0]);
+  T nrm = T(0);
   for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
-    double xv = 0.0, av = 0.0, xw = 0.0, aw = 0.0;
+    T xv = T(0), av = T(0), xw = T(0), aw = T(0);
     int j = 0;
     for (; j + 2 <= k; j += 2) {
-      const double v0 = V[int64_t(j) * ldv + i], v1 = V[int64_t(j + 1) * ldv + i];
-      const double a0 = AV[int64_t(j) * ldv + i], a1 = AV[int64_t(j + 1) * ldv + i];
+      const T v0 = V[int64_t(j) * ldv + i], v1 = V[int64_t(j + 1) * ldv + i];
+      const T a0 = AV[int64_t(j) * ldv + i], a1 = AV[int64_t(j + 1) * ldv + i];
       xv = fma(ss[j], v0, xv);
       av = fma(ss[j], a0, av);
       xw = fma(ss[j + 1], v1, xw);
@@ -153,21 +166,21 @@ __global__ void __launch_bounds__(DT) ritz_kernel(const double* __restrict__ V, 
     }
     xv += xw;
     av += aw;
-    const double r = av - theta * xv;
+    const T r = av - theta * xv;
     x[i] = xv;
     ax[i] = av;
-    double tv = r;
+    T tv = r;
     if (precond) {
-      double den = diag[i] - theta;
-      const double floor = 1e-2;
-      if (fabs(den) < floor) den = den >= 0.0 ? floor : -floor;
+      T den = diag[i] - theta;
+      const T floor = T(1e-2);
+      if (abs(den) < floor) den = den >= T(0) ? floor : -floor;
       tv = r / den;
     }
     t[i] = tv;
     nrm = fma(r, r, nrm);
   }
-  nrm = block_sum(nrm, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = nrm;
+  const double tot = block_sum(double(nrm), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
 // after a restart to the single Ritz vector x: H = [[theta]], Ritz coefficients s = [1]
@@ -187,6 +200,7 @@ struct DavWs {
   void* mv;
   size_t mv_bytes;
   double *T1, *T2;  // FP64-class matvec scratch (also used by the anchored phase)
+  float* diag32;     // diag(H) in FP32 for the mixed form's first phase
   void* oz;         // operand slices of the tensor-core FP64-class GEMMs
   size_t oz_bytes;
 };
@@ -212,7 +226,7 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
          oHw = take(size_t(mb) * mb * 8), oev = take(size_t(mb) * 8), oevec = take(size_t(mb) * mb * 8),
          ojw = take(2 * size_t(mb) * mb * 8), opart = take(size_t(mb + 1) * nch * 8),
          oscal = take(size_t(4 * MAXB) * 8), oT1 = take(ne * 8), oT2 = take(ne * 8), omv = take(mv_bytes),
-         ooz = take(oz_bytes);
+         ooz = take(oz_bytes), od32 = take(precision == TNX_BF16X3 ? size_t(n) * 4 : 0);
   if (w && base && off <= size) {
     char* b = static_cast<char*>(base);
     w->V = reinterpret_cast<double*>(b + oV);
@@ -234,15 +248,17 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
     w->mv_bytes = mv_bytes;
     w->oz = oz_bytes ? static_cast<void*>(b + ooz) : nullptr;
     w->oz_bytes = oz_bytes;
+    w->diag32 = precision == TNX_BF16X3 ? reinterpret_cast<float*>(b + od32) : nullptr;
   }
   return off;
 }
 
 // h[0..k) = V[0..k) . w
-int dots(const double* V, int64_t ldv, int k, const double* w, int64_t n, double* part, double* out,
+template <typename T>
+int dots(const T* V, int64_t ldv, int k, const T* w, int64_t n, double* part, double* out,
          int out_stride, double* out2, int out2_stride, cudaStream_t st, const double* gate = nullptr) {
   const int nch = nchunk_for(n);
-  dots_kernel<<<dim3(nch, k), DT, 0, st>>>(V, ldv, w, n, part, nch, gate);
+  dots_kernel<T><<<dim3(nch, k), DT, 0, st>>>(V, ldv, w, n, part, nch, gate);
   TNX_LAUNCH_CHECK();
   reduce_kernel<<<k, DT, 0, st>>>(part, nch, out, out_stride, out2, out2_stride);
   TNX_LAUNCH_CHECK();
@@ -273,10 +289,29 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     TNX_TRY(mixed_prepare(L, R, chi_l, d, chi_r, dl, dr, w.mv, st));
     mixed_flag(w.mv, chi_l, d, chi_r, dl, dr, &dflag);
   }
-  auto matvec = [&](const double* in, double* out) -> int {
-    if (mixed) return mixed_apply(W, in, out, chi_l, d, chi_r, dl, dr, w.mv, st);
-    return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, precision == TNX_DF64, w.oz,
-                       w.oz_bytes);
+  // Vector storage of the current phase. The mixed form's first phase (split-BF16 products,
+  // converged only to ~3e-6) keeps its basis, Ritz vector and residual in FP32 views of the
+  // same buffers: half the bytes, and FP32 instead of FP64-pipe arithmetic in every vector
+  // kernel; the anchored phase restarts from the Ritz vector converted to FP64.
+  struct Vecs32 {
+    float *V, *AV, *x, *ax, *t, *diag;
+  };
+  struct Vecs64 {
+    double *V, *AV, *x, *ax, *t, *diag;
+  };
+  const Vecs32 v32{reinterpret_cast<float*>(w.V), reinterpret_cast<float*>(w.AV), reinterpret_cast<float*>(w.x),
+                   reinterpret_cast<float*>(w.ax), reinterpret_cast<float*>(w.t), w.diag32};
+  const Vecs64 v64{w.V, w.AV, w.x, w.ax, w.t, w.diag};
+  const bool f32 = mixed && w.diag32 != nullptr;
+  auto matvec = [&](auto* in, auto* out) -> int {
+    using T = std::remove_const_t<std::remove_pointer_t<decltype(in)>>;
+    if constexpr (std::is_same_v<T, float>) {
+      return mixed_apply_f32(W, in, out, chi_l, d, chi_r, dl, dr, w.mv, st);
+    } else {
+      if (mixed) return mixed_apply(W, in, out, chi_l, d, chi_r, dl, dr, w.mv, st);
+      return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, precision == TNX_DF64, w.oz,
+                         w.oz_bytes);
+    }
   };
   int hflag = 0;
   double* h = w.scal;               // [MAXB]
@@ -284,17 +319,24 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   double* rn2 = w.scal + MAXB + 2;  // ||r||^2
   double host[4];
 
-  TNX_CUDA(cudaMemcpyAsync(w.t, x_io, n * 8, cudaMemcpyDeviceToDevice, st));
   if (int e = tnx_diag1(L, W, R, w.diag, chi_l, d, chi_r, dl, dr, st); e != TNX_OK) return e;
+  if (f32) {
+    convert_kernel<double, float><<<sblocks, DT, 0, st>>>(x_io, v32.t, n);
+    TNX_LAUNCH_CHECK();
+    convert_kernel<double, float><<<sblocks, DT, 0, st>>>(w.diag, w.diag32, n);
+    TNX_LAUNCH_CHECK();
+  } else {
+    TNX_CUDA(cudaMemcpyAsync(w.t, x_io, n * 8, cudaMemcpyDeviceToDevice, st));
+  }
 
   int k = 0, iters = 0, precond = 1;
   double theta = 0.0, rnorm = INFINITY, c0 = 1.0;
 
   // Rayleigh-Ritz on V[0..k), Ritz vector x, AV-combination ax, residual norm and the next
   // direction t; reads theta, ||r|| and the Ritz coefficient of V[0] back to the host.
-  auto rayleigh_ritz = [&]() -> int {
+  auto rayleigh_ritz = [&](const auto& vs) -> int {
     TNX_TRY(rr_lowest_f64(w.Hm, k, mb, w.evals, w.evecs, st));
-    ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, precond, w.x, w.ax, w.t, n,
+    ritz_kernel<<<nch, DT, 0, st>>>(vs.V, vs.AV, n, k, w.evecs, w.evals, vs.diag, precond, vs.x, vs.ax, vs.t, n,
                                     w.part, nch);
     TNX_LAUNCH_CHECK();
     reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
@@ -323,15 +365,16 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // product AV[0] = H V[0] is FP64-class exact, and row 0 of the projected matrix is taken as
   // AV[0] . V[k] (exact, H being symmetric) instead of V[0] . AV[k]. `*fell_in` reports a
   // direction that vanished against the basis (nothing expanded).
-  auto expand = [&](bool anchored, bool* fell_in) -> int {
+  auto expand = [&](const auto& vs, bool anchored, bool* fell_in) -> int {
+    using T = std::remove_pointer_t<decltype(vs.V)>;
     *fell_in = false;
-    double* vk = w.V + int64_t(k) * n;
-    TNX_CUDA(cudaMemcpyAsync(vk, w.t, n * 8, cudaMemcpyDeviceToDevice, st));
-    TNX_TRY(dots(vk, n, 1, vk, n, w.part, nrm2, 1, nullptr, 0, st));
+    T* vk = vs.V + int64_t(k) * n;
+    TNX_CUDA(cudaMemcpyAsync(vk, vs.t, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    TNX_TRY(dots<T>(vk, n, 1, vk, n, w.part, nrm2, 1, nullptr, 0, st));
     for (int pass = 0; pass < 2 && k > 0; ++pass) {
       const double* gate = pass == 0 ? nullptr : nrm2;
-      TNX_TRY(dots(w.V, n, k, vk, n, w.part, h, 1, nullptr, 0, st, gate));
-      update_kernel<<<nch, DT, 0, st>>>(w.V, n, k, h, vk, n, w.part, nch, gate);
+      TNX_TRY(dots<T>(vs.V, n, k, vk, n, w.part, h, 1, nullptr, 0, st, gate));
+      update_kernel<T><<<nch, DT, 0, st>>>(vs.V, n, k, h, vk, n, w.part, nch, gate);
       TNX_LAUNCH_CHECK();
       reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, nrm2 + 1, 1, nullptr, 0);
       TNX_LAUNCH_CHECK();
@@ -347,21 +390,23 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       *fell_in = true;
       return TNX_OK;
     }
-    scale_kernel<<<sblocks, DT, 0, st>>>(vk, n, nrm2 + 1);
+    scale_kernel<T><<<sblocks, DT, 0, st>>>(vk, n, nrm2 + 1);
     TNX_LAUNCH_CHECK();
-    double* avk = w.AV + int64_t(k) * n;
+    T* avk = vs.AV + int64_t(k) * n;
     TNX_TRY(matvec(vk, avk));
     ++iters;
-    TNX_TRY(dots(w.V, n, k + 1, avk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
-    if (anchored && k > 0) TNX_TRY(dots(w.AV, n, 1, vk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
+    TNX_TRY(dots<T>(vs.V, n, k + 1, avk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
+    if (anchored && k > 0)
+      TNX_TRY(dots<T>(vs.AV, n, 1, vk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
     ++k;
-    return rayleigh_ritz();
+    return rayleigh_ritz(vs);
   };
 
   // thick restart with the current Ritz vector
-  auto restart = [&]() -> int {
-    TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
-    TNX_CUDA(cudaMemcpyAsync(w.AV, w.ax, n * 8, cudaMemcpyDeviceToDevice, st));
+  auto restart = [&](const auto& vs) -> int {
+    using T = std::remove_pointer_t<decltype(vs.V)>;
+    TNX_CUDA(cudaMemcpyAsync(vs.V, vs.x, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    TNX_CUDA(cudaMemcpyAsync(vs.AV, vs.ax, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
     restart_kernel<<<1, 1, 0, st>>>(w.Hm, w.evals, w.evecs);
     TNX_LAUNCH_CHECK();
     k = 1;
@@ -384,12 +429,16 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   const double mixed_handover = 3e-6, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
   for (;;) {
     bool fell_in = false;
-    TNX_TRY(expand(false, &fell_in));
+    TNX_TRY(f32 ? expand(v32, false, &fell_in) : expand(v64, false, &fell_in));
     if (fell_in) {
       if (precond) {  // preconditioned direction fell inside the basis: retry with r
         precond = 0;
-        ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, 0, w.x, w.ax, w.t, n,
-                                        w.part, nch);
+        if (f32)
+          ritz_kernel<<<nch, DT, 0, st>>>(v32.V, v32.AV, n, k, w.evecs, w.evals, v32.diag, 0, v32.x, v32.ax, v32.t,
+                                          n, w.part, nch);
+        else
+          ritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, n, k, w.evecs, w.evals, w.diag, 0, w.x, w.ax, w.t, n, w.part,
+                                          nch);
         TNX_LAUNCH_CHECK();
         continue;
       }
@@ -414,7 +463,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     }
     if (iters >= max_iter) break;
     precond = 1;
-    if (k == mb) TNX_TRY(restart());
+    if (k == mb) TNX_TRY(f32 ? restart(v32) : restart(v64));
   }
   if (mixed) {
     // Anchored phase. One double-FP32 matvec gives AV[0] = H x exactly for the current Ritz
@@ -429,13 +478,18 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     const double eps_h = 3e-5;  // bound on the split-BF16 matvec error relative to |H| ~ 2|theta|
     converged = false;
     for (int anchor = 0;; ++anchor) {
-      TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+      if (anchor == 0 && f32) {
+        convert_kernel<float, double><<<sblocks, DT, 0, st>>>(v32.x, w.V, n);
+        TNX_LAUNCH_CHECK();
+      } else {
+        TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+      }
       TNX_TRY(matvec1_f64(L, W, R, w.V, w.AV, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true, w.oz,
                           w.oz_bytes));
       TNX_TRY(dots(w.V, n, 1, w.AV, n, w.part, w.Hm, 1, nullptr, 0, st));
       k = 1;
       precond = 1;
-      TNX_TRY(rayleigh_ritz());
+      TNX_TRY(rayleigh_ritz(v64));
       double drift = 0.0;  // sum of |c| over restarts inside this anchor
       auto bound_ok = [&]() {
         const double c = sqrt(fmax(1.0 - c0 * c0, 0.0));
@@ -448,17 +502,20 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       if (anchor >= max_anchor || iters >= max_iter) break;
       best = rnorm;
       best_it = iters;
-      // The bound only decides whether a converged residual is accepted; while the residual is
-      // still large the phase keeps expanding (it is then a Davidson whose row 0 is exact) and
-      // re-anchors on stagnation or once the Ritz vector has moved far from the anchor.
+      // The bound decides whether a converged residual is accepted and, within 100x of the
+      // target, when to refresh the anchor; while the residual is still large the phase keeps
+      // expanding (a Davidson whose row 0 is exact) and re-anchors on stagnation or once the
+      // Ritz vector has moved far from the anchor.
       for (;;) {
         bool fell_in = false;
-        TNX_TRY(expand(true, &fell_in));
+        TNX_TRY(expand(v64, true, &fell_in));
         if (fell_in) break;
         if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta))) {
           if (bound_ok()) converged = true;
           break;
         }
+        // close to the target but the anchor no longer vouches for the residual: refresh it
+        if (!bound_ok() && rnorm < 100.0 * mixed_rtol * fmax(1.0, fabs(theta))) break;
         if (drift + sqrt(fmax(1.0 - c0 * c0, 0.0)) > 0.3) break;
         if (rnorm < 0.9 * best) {
           best = rnorm;
@@ -469,7 +526,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
         if (iters >= max_iter) break;
         if (k == mb) {
           drift += sqrt(fmax(1.0 - c0 * c0, 0.0));
-          TNX_TRY(restart());
+          TNX_TRY(restart(v64));
         }
       }
       if (converged || iters >= max_iter) break;

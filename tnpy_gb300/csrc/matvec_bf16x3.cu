@@ -176,14 +176,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 // ---------------------------------------------------------------- operand preparation
 // dst_hi/lo[c][r] (row pitch ldp) = split(src[r][c]) for r < rows; zeros for rows <= r < ldp.
 // src is row-major rows x cols (FP64).
-__global__ void split_transpose_kernel(const double* __restrict__ src, int64_t rows, int64_t cols,
+template <typename T>
+__global__ void split_transpose_kernel(const T* __restrict__ src, int64_t rows, int64_t cols,
                                        __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
                                        int64_t ldp) {
   __shared__ double tile[32][33];
   const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
     const int64_t r = r0 + k, c = c0 + threadIdx.x;
-    tile[k][threadIdx.x] = (r < rows && c < cols) ? src[r * cols + c] : 0.0;
+    tile[k][threadIdx.x] = (r < rows && c < cols) ? double(src[r * cols + c]) : 0.0;
   }
   __syncthreads();
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
@@ -394,10 +395,10 @@ int mixed_prepare(const double* L, const double* R, int64_t chi_l, int64_t d, in
   mixed_layout(chi_l, d, chi_r, dl, dr, align1024(scratch), &m);
   dim3 tb(32, 8);
   // A1[(w a')][a] = L[a][(w a')]: src rows = chi_l, cols = dl*chi_l, pitch K1p
-  split_transpose_kernel<<<tgrid(m.K1p, m.M1), tb, 0, st>>>(L, chi_l, m.M1, m.a1h, m.a1l, m.K1p);
+  split_transpose_kernel<double><<<tgrid(m.K1p, m.M1), tb, 0, st>>>(L, chi_l, m.M1, m.a1h, m.a1l, m.K1p);
   TNX_LAUNCH_CHECK();
   // B3[c'][(c v)] = R[(c v)][c']: src rows = chi_r*dr, cols = chi_r, pitch K3p
-  split_transpose_kernel<<<tgrid(m.K3p, m.N3), tb, 0, st>>>(R, chi_r * dr, chi_r, m.b3h, m.b3l, m.K3p);
+  split_transpose_kernel<double><<<tgrid(m.K3p, m.N3), tb, 0, st>>>(R, chi_r * dr, chi_r, m.b3h, m.b3l, m.K3p);
   TNX_LAUNCH_CHECK();
   if (m.K3p > chi_r * dr) {
     zero_pad_kernel<<<152, 256, 0, st>>>(m.a3h, m.a3l, m.M3, chi_r * dr, m.K3p);
@@ -407,14 +408,15 @@ int mixed_prepare(const double* L, const double* R, int64_t chi_l, int64_t d, in
   return TNX_OK;
 }
 
-// One matvec with prepared L / R operands.
-int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
-                int64_t dr, void* scratch, cudaStream_t st) {
+// One matvec with prepared L / R operands; x and y FP64 or FP32 (T).
+template <typename T>
+int mixed_apply_t(const double* W, const T* x, T* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                  int64_t dr, void* scratch, cudaStream_t st) {
   MixedLayout m;
   mixed_layout(chi_l, d, chi_r, dl, dr, align1024(scratch), &m);
   dim3 tb(32, 8);
   // B1[(s c)][a] = x[a][(s c)]
-  split_transpose_kernel<<<tgrid(m.K1p, m.N1), tb, 0, st>>>(x, chi_l, m.N1, m.b1h, m.b1l, m.K1p);
+  split_transpose_kernel<T><<<tgrid(m.K1p, m.N1), tb, 0, st>>>(x, chi_l, m.N1, m.b1h, m.b1l, m.K1p);
   TNX_LAUNCH_CHECK();
   // step 1: T1 (FP32) = A1 . B1^T
   if (m.N1 >= 256)
@@ -433,10 +435,20 @@ int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int6
                                                                  int(dl), int(dr), m.K3p);
     TNX_LAUNCH_CHECK();
   }
-  // step 3: y (FP64) = A3 . B3^T
-  TNX_TRY(launch_gemm<128>(m.a3h, m.a3l, m.b3h, m.b3l, int(m.M3), int(m.N3), int(m.K3p), y, m.N3, true, m.flag,
-                           st, chi_r * dr));
+  // step 3: y = A3 . B3^T (FP32 accumulators written as T)
+  TNX_TRY(launch_gemm<128>(m.a3h, m.a3l, m.b3h, m.b3l, int(m.M3), int(m.N3), int(m.K3p), y, m.N3,
+                           sizeof(T) == 8, m.flag, st, chi_r * dr));
   return TNX_OK;
+}
+
+int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                int64_t dr, void* scratch, cudaStream_t st) {
+  return mixed_apply_t<double>(W, x, y, chi_l, d, chi_r, dl, dr, scratch, st);
+}
+
+int mixed_apply_f32(const double* W, const float* x, float* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                    int64_t dr, void* scratch, cudaStream_t st) {
+  return mixed_apply_t<float>(W, x, y, chi_l, d, chi_r, dl, dr, scratch, st);
 }
 
 int mixed_flag(void* scratch, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int** flag) {

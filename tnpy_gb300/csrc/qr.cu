@@ -424,8 +424,11 @@ unsigned blocks_for(int64_t total) {
   return unsigned(b < 1 ? 1 : b);
 }
 
+// Two scratch sets (Vp / W1 / W2 / part): set 0 for the caller's stream, set 1 for the
+// look-ahead stream of the factorisation.
 struct QrWs {
   double *F, *Qc, *tau, *T, *Vp, *W1, *W2, *part;
+  double *Vp2, *W1b, *W2b, *partb;
 };
 constexpr int QBMAX = 64;  // widest panel
 constexpr int QR_SPLIT_MAX = 16;
@@ -441,7 +444,8 @@ size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
   const int64_t np = (n + QBMAX - 1) / QBMAX;
   size_t oF = take(m * n * 8), oQ = take(m * n * 8), otau = take(np * QBMAX * 8),
          oT = take(np * QBMAX * QBMAX * 8), oV = take(m * QBMAX * 8), oW1 = take(n * QBMAX * 8),
-         oW2 = take(n * QBMAX * 8), oP = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8);
+         oW2 = take(n * QBMAX * 8), oP = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8), oV2 = take(m * QBMAX * 8),
+         oW1b = take(n * QBMAX * 8), oW2b = take(n * QBMAX * 8), oPb = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8);
   if (w && base) {
     char* b = static_cast<char*>(base);
     w->F = reinterpret_cast<double*>(b + oF);
@@ -452,6 +456,10 @@ size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
     w->W1 = reinterpret_cast<double*>(b + oW1);
     w->W2 = reinterpret_cast<double*>(b + oW2);
     w->part = reinterpret_cast<double*>(b + oP);
+    w->Vp2 = reinterpret_cast<double*>(b + oV2);
+    w->W1b = reinterpret_cast<double*>(b + oW1b);
+    w->W2b = reinterpret_cast<double*>(b + oW2b);
+    w->partb = reinterpret_cast<double*>(b + oPb);
   }
   return off;
 }
@@ -574,33 +582,91 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
   return rc;
 }
 
+// C -= V T^T V^T C for the mp x nc column-major block C (ld m): the trailing update of one
+// panel (V: mp x nb column-major in Vp, T: column-major ld NB)
+int apply_panel_t(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int64_t nc,
+                  double* W1, double* W2, double* part, cudaStream_t st, bool df) {
+  if (nc <= 0) return TNX_OK;
+  // Row-major views: C (column-major mp x nc, ld m) is C^T (nc x mp, ld m), V is V^T (nb x mp).
+  // W1 (nb x nc) = V^T C  (short output rows, long K: split over K)
+  TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, Vp, mp, C, m, 0.0, W1, nc, qr_nsplit(mp), part, st, df));
+  // W2 = T^T W1   (T column-major with ld NB is T^T row-major)
+  TNX_TRY(gemm_fp64_class(df, false, false, nb, nc, nb, 1.0, Tp, NB, 0, W1, nc, 0, 0.0, W2, nc, 0, 1, st));
+  // C -= V W2, i.e. C^T -= W2^T V^T
+  TNX_TRY(gemm_fp64_class(df, true, false, nc, mp, nb, -1.0, W2, nc, 0, Vp, mp, 0, 1.0, C, m, 0, 1, st));
+  return TNX_OK;
+}
+
+// Look-ahead stream and its two events, one set per host thread and device, created on first use
+// and kept for the thread's lifetime.
+struct LookAhead {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_v = nullptr, ev_r = nullptr;
+};
+
+int look_ahead(LookAhead** out) {
+  constexpr int MAXDEV = 64;
+  thread_local LookAhead la[MAXDEV];
+  int dev = 0;
+  TNX_CUDA(cudaGetDevice(&dev));
+  TNX_CHECK_ARG(dev >= 0 && dev < MAXDEV, "device index %d out of range", dev);
+  LookAhead& l = la[dev];
+  if (!l.aux) {
+    TNX_CUDA(cudaStreamCreateWithFlags(&l.aux, cudaStreamNonBlocking));
+    TNX_CUDA(cudaEventCreateWithFlags(&l.ev_v, cudaEventDisableTiming));
+    TNX_CUDA(cudaEventCreateWithFlags(&l.ev_r, cudaEventDisableTiming));
+  }
+  *out = &l;
+  return TNX_OK;
+}
+
 }  // namespace
 
 // Factor the column-major m x n matrix in w.F (m >= n) and form Q (column-major) in w.Qc.
+//
+// Factorisation with look-ahead: after panel p is factored, the caller's stream updates only the
+// next panel's columns with H_p and factors panel p+1, while the look-ahead stream applies H_p to
+// all columns beyond panel p+1 (the bulk of the flops); the 16 SMs of a panel no longer leave
+// the rest of the GPU idle. Panel p+2's columns (part of that bulk) are used only after the
+// look-ahead stream's update of step p has completed. V is double-buffered between the streams.
 int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false) {
   const PanelPlan pp = plan_panels(m);
   const int NB = pp.nb;
   const int64_t np = (n + NB - 1) / NB;
+  LookAhead* la = nullptr;
+  TNX_TRY(look_ahead(&la));
+  // the look-ahead stream starts after everything queued on the caller's stream
+  TNX_CUDA(cudaEventRecord(la->ev_r, st));
+  TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_r, 0));
+  TNX_TRY(factor_panel(pp, w.F, m, 0, int(n < NB ? n : NB), w.tau, w.T, st));
   for (int64_t p = 0; p < np; ++p) {
     const int64_t j0 = p * NB;
     const int nb = int(n - j0 < NB ? n - j0 : NB);
     double* Tp = w.T + p * NB * NB;  // column-major nb x nb, ld NB
-    TNX_TRY(factor_panel(pp, w.F, m, j0, nb, w.tau + p * NB, Tp, st));
     const int64_t mp = m - j0, nc = n - j0 - nb;
-    if (nc > 0) {
-      panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, w.Vp);
-      TNX_LAUNCH_CHECK();
-      // Row-major views: C (column-major mp x nc, ld m) is C^T (nc x mp, ld m), V is V^T (nb x mp).
-      double* C = w.F + (j0 + nb) * m + j0;
-      // W1 (nb x nc) = V^T C  (short output rows, long K: split over K)
-      TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, w.Vp, mp, C, m, 0.0, w.W1, nc, qr_nsplit(mp), w.part,
-                              st, df));
-      // W2 = T^T W1   (T column-major with ld NB is T^T row-major)
-      TNX_TRY(gemm_fp64_class(df, false, false, nb, nc, nb, 1.0, Tp, NB, 0, w.W1, nc, 0, 0.0, w.W2, nc, 0, 1, st));
-      // C -= V W2, i.e. C^T -= W2^T V^T
-      TNX_TRY(gemm_fp64_class(df, true, false, nc, mp, nb, -1.0, w.W2, nc, 0, w.Vp, mp, 0, 1.0, C, m, 0, 1, st));
+    if (nc <= 0) break;
+    double* Vp = (p & 1) ? w.Vp2 : w.Vp;
+    panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, Vp);
+    TNX_LAUNCH_CHECK();
+    const int nb1 = int(nc < NB ? nc : NB);  // next panel
+    const int64_t rest = nc - nb1;
+    double* Cn = w.F + (j0 + nb) * m + j0;
+    if (rest > 0) {
+      TNX_CUDA(cudaEventRecord(la->ev_v, st));  // V_p, T_p ready; panel p+2's columns updated by H_{p-1}
+      TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_v, 0));
+      TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, la->aux, df));
+    }
+    TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, st, df));
+    TNX_TRY(factor_panel(pp, w.F, m, j0 + nb, nb1, w.tau + (p + 1) * NB, w.T + (p + 1) * NB * NB, st));
+    if (rest > 0) {
+      // the next step reads panel p+2's columns and rewrites the other V buffer
+      TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));
+      TNX_CUDA(cudaStreamWaitEvent(st, la->ev_r, 0));
     }
   }
+  // join the look-ahead stream back (also when it received no work: keeps stream capture balanced)
+  TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));
+  TNX_CUDA(cudaStreamWaitEvent(st, la->ev_r, 0));
   // Q = H_0 H_1 ... [I; 0]: apply panels last to first to the columns >= j0
   eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.Qc, m, n);
   TNX_LAUNCH_CHECK();

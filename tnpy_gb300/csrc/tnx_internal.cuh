@@ -191,6 +191,9 @@ int mixed_prepare(const double* L, const double* R, int64_t chi_l, int64_t d, in
                   void* scratch, cudaStream_t st);
 int mixed_apply(const double* W, const double* x, double* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
                 int64_t dr, void* scratch, cudaStream_t st);
+// the same product with FP32 input / output vectors
+int mixed_apply_f32(const double* W, const float* x, float* y, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                    int64_t dr, void* scratch, cudaStream_t st);
 int mixed_flag(void* scratch, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int** flag);
 
 // ---- dense symmetric eigensolver ------------------------------------------------------
