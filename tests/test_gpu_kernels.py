@@ -108,6 +108,56 @@ def test_qr(cuda, m, n):
     assert np.allclose(np.tril(r, -1), 0)
 
 
+@pytest.mark.parametrize("m,n", [(300, 300), (1100, 700)])
+def test_qr_stale_workspace(cuda, m, n):
+    """The QR reads no scratch it has not written: the workspace is filled with NaN first
+    (two outer blocks of 256 columns and a ragged third / a ragged second)."""
+    import tnpy_gb300.kernels as K
+    from tnpy_gb300._lib import lib
+
+    rng = np.random.RandomState(7)
+    a = rng.standard_normal((m, n))
+    _poison_workspace(lib.tnx_qr_workspace_bytes(m, n), cuda)
+    q, r = K.qr(_t(a, cuda))
+    q, r = q.cpu().numpy(), r.cpu().numpy()
+    np.testing.assert_allclose(q.T @ q, np.eye(n), atol=1e-13)
+    np.testing.assert_allclose(q @ r, a, atol=1e-12 * np.abs(a).max() * np.sqrt(n))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gauge_move_stale_workspace(cuda, precision):
+    """Gauge move (chi 600 x 2 x 600 site, both directions) on a NaN-filled workspace."""
+    import tnpy_gb300.kernels as K
+    from tnpy_gb300._lib import lib
+
+    rng = np.random.RandomState(5)
+    chi = 600
+    for direction in (1, -1):
+        a = rng.standard_normal((chi, 2, chi))
+        nbr = rng.standard_normal((chi, 2, 8)) if direction == 1 else rng.standard_normal((8, 2, chi))
+        ta, tn = _t(a, cuda), _t(nbr, cuda)
+        _poison_workspace(lib.tnx_gauge_move_workspace_bytes(direction, chi, 2, chi, 8), cuda)
+        K.gauge_move(direction, ta, tn, precision=precision)
+        q = ta.cpu().numpy().reshape(chi * 2, chi) if direction == 1 else ta.cpu().numpy().reshape(chi, 2 * chi).T
+        np.testing.assert_allclose(q.T @ q, np.eye(chi), atol=1e-12)
+        # the two-site contraction is unchanged by the move
+        before = np.tensordot(a, nbr, axes=([2], [0])) if direction == 1 else np.tensordot(nbr, a, axes=([2], [0]))
+        after = (np.tensordot(ta.cpu().numpy(), tn.cpu().numpy(), axes=([2], [0])) if direction == 1
+                 else np.tensordot(tn.cpu().numpy(), ta.cpu().numpy(), axes=([2], [0])))
+        np.testing.assert_allclose(after, before, atol=1e-11 * np.abs(before).max())
+
+
+def _poison_workspace(nbytes, device):
+    """Fill the library's scratch buffer for the current stream with 0xFF bytes (NaN doubles)."""
+    import torch
+
+    from tnpy_gb300._lib import Workspace
+
+    Workspace.get(nbytes, device)
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    Workspace._bufs[(idx, torch.cuda.current_stream(idx).cuda_stream)].fill_(255)
+
+
 def test_qr_rank_deficient(cuda):
     import tnpy_gb300.kernels as K
 

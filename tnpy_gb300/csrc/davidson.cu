@@ -127,6 +127,29 @@ __global__ void scale_kernel(T* __restrict__ w, int64_t n, const double* __restr
     w[i] *= s;
 }
 
+// part[block] = max |v| over the block's grid-stride share; then max over the partials (one block)
+__global__ void __launch_bounds__(DT) absmax_kernel(const double* __restrict__ v, int64_t n, double* __restrict__ part,
+                                                   int nchunk) {
+  __shared__ double sh[DT / 32];
+  double m = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) m = fmax(m, fabs(v[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < DT / 32; ++w) m = fmax(m, sh[w]);
+    part[blockIdx.x] = m;
+  }
+}
+
+__global__ void max_reduce_kernel(const double* __restrict__ part, int nchunk, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int c = 0; c < nchunk; ++c) m = fmax(m, part[c]);
+    out[0] = m;
+  }
+}
+
 // out = T(in) (precision change of one vector)
 template <typename Tin, typename Tout>
 __global__ void convert_kernel(const Tin* __restrict__ in, Tout* __restrict__ out, int64_t n) {
@@ -472,10 +495,19 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     // split-BF16 error E ~ 3e-5 |H| enters the Ritz value only through c^T E c and the
     // residual through E c, where c (|c| = sqrt(1 - c0^2)) is the small part of the Ritz
     // vector outside x. The residual of the anchored Ritz pair is therefore FP64-class
-    // while 3e-5 * 2|theta| * |c| stays below half the target; otherwise (or on stagnation)
-    // the phase re-anchors at the current Ritz vector with another double-FP32 matvec.
+    // while 3e-5 |H| |c| stays below half the target; otherwise (or on stagnation) the phase
+    // re-anchors at the current Ritz vector with another FP64-class matvec.
     const int max_anchor = 6;
-    const double eps_h = 3e-5;  // bound on the split-BF16 matvec error relative to |H| ~ 2|theta|
+    const double eps_h = 3e-5;  // bound on the split-BF16 matvec error relative to |H|
+    // |H| for the bound: max(2 |theta|, max |diag H|); the diagonal alone is a lower bound of the
+    // spectral radius and catches operators whose lowest eigenvalue is small against their width
+    absmax_kernel<<<nch, DT, 0, st>>>(w.diag, n, w.part, nch);
+    TNX_LAUNCH_CHECK();
+    max_reduce_kernel<<<1, 32, 0, st>>>(w.part, nch, w.scal + MAXB + 3);
+    TNX_LAUNCH_CHECK();
+    double hdiag = 0.0;
+    TNX_CUDA(cudaMemcpyAsync(&hdiag, w.scal + MAXB + 3, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaStreamSynchronize(st));
     converged = false;
     for (int anchor = 0;; ++anchor) {
       if (anchor == 0 && f32) {
@@ -484,6 +516,11 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       } else {
         TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
       }
+      // unit norm in FP64: the Rayleigh-Ritz below treats the basis as orthonormal, and a
+      // Ritz vector formed in FP32 is normalised only to ~1e-8 (an offset of theta that size)
+      TNX_TRY(dots(w.V, n, 1, w.V, n, w.part, nrm2, 1, nullptr, 0, st));
+      scale_kernel<double><<<sblocks, DT, 0, st>>>(w.V, n, nrm2);
+      TNX_LAUNCH_CHECK();
       TNX_TRY(matvec1_f64(L, W, R, w.V, w.AV, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true, w.oz,
                           w.oz_bytes));
       TNX_TRY(dots(w.V, n, 1, w.AV, n, w.part, w.Hm, 1, nullptr, 0, st));
@@ -493,7 +530,8 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       double drift = 0.0;  // sum of |c| over restarts inside this anchor
       auto bound_ok = [&]() {
         const double c = sqrt(fmax(1.0 - c0 * c0, 0.0));
-        return eps_h * 2.0 * fmax(1.0, fabs(theta)) * (drift + c) <= 0.5 * mixed_rtol * fmax(1.0, fabs(theta));
+        const double hs = fmax(fmax(2.0 * fabs(theta), hdiag), 1.0);
+        return eps_h * hs * (drift + c) <= 0.5 * mixed_rtol * fmax(1.0, fabs(theta));
       };
       if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta))) {
         converged = true;
