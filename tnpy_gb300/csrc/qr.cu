@@ -17,8 +17,10 @@
 
 #include <cstdlib>
 #include <mutex>
+#include <string>
 
 #include "tnx_internal.cuh"
+#include "qr_panel_df.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -475,12 +477,24 @@ struct PanelKernelInfo {
   size_t max_dyn = 0;
 };
 
-template <int NB, int CL>
+// DF selects the double-FP32 panel (FP64-class modes), otherwise the FP64 one
+using PanelFn = void (*)(double*, int64_t, int64_t, int, int, double*, double*);
+template <int NB, int CL, bool DF>
+PanelFn panel_fn() {
+  if constexpr (DF) return qrdf::panel_df_kernel<NB, CL>;
+  else return panel_cl_kernel<NB, CL>;
+}
+template <bool DF>
+constexpr int panel_threads() {
+  return DF ? qrdf::DPT : PT;
+}
+
+template <int NB, int CL, bool DF>
 const PanelKernelInfo& panel_info() {
   static PanelKernelInfo info;
   static std::once_flag once;
   std::call_once(once, [] {
-    auto k = panel_cl_kernel<NB, CL>;
+    PanelFn k = panel_fn<NB, CL, DF>();
     cudaFuncAttributes fa{};
     int dev = 0, optin = 0;
     if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
@@ -501,7 +515,7 @@ const PanelKernelInfo& panel_info() {
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(CL);
-    cfg.blockDim = dim3(PT);
+    cfg.blockDim = dim3(panel_threads<DF>());
     cfg.dynamicSmemBytes = dyn;
     cfg.attrs = at;
     cfg.numAttrs = 1;
@@ -516,10 +530,10 @@ const PanelKernelInfo& panel_info() {
   return info;
 }
 
-template <int NB, int CL>
+template <int NB, int CL, bool DF>
 int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* T, cudaStream_t st) {
   const int64_t rpc = (m - j0 + CL - 1) / CL;
-  const int ld = panel_ld(rpc, PT / NB);
+  const int ld = panel_ld(rpc, panel_threads<DF>() / NB);
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -527,43 +541,53 @@ int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* 
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.gridDim = dim3(CL);
-  cfg.blockDim = dim3(PT);
+  cfg.blockDim = dim3(panel_threads<DF>());
   cfg.dynamicSmemBytes = size_t(NB + 2) * ld * sizeof(double);
   cfg.stream = st;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  TNX_CUDA(cudaLaunchKernelEx(&cfg, panel_cl_kernel<NB, CL>, F, m, j0, nb, ld, tau, T));
+  TNX_CUDA(cudaLaunchKernelEx(&cfg, panel_fn<NB, CL, DF>(), F, m, j0, nb, ld, tau, T));
   TNX_LAUNCH_CHECK();
   return TNX_OK;
 }
 
-// Panel plan of one QR: width nb (64 or 32) and cluster size cl (16 or 8; 0 = one-CTA panel,
-// for panels too tall for a cluster's shared memory). Wider panels give the trailing-update
-// GEMMs a longer K; 16-CTA clusters (where the device schedules them) spread the panel's FP64
-// arithmetic over twice the SMs of the portable 8.
-// TNX_QR_CLUSTER=8 or 16 restricts the cluster size (tuning).
+// Panel plan of one QR: width nb (64 or 32), cluster size cl (16 or 8; 0 = one-CTA panel,
+// for panels too tall for a cluster's shared memory) and arithmetic (df: the double-FP32 panel
+// of the FP64-class modes). Wider panels give the trailing-update GEMMs a longer K; 16-CTA
+// clusters (where the device schedules them) spread the panel over twice the SMs of the
+// portable 8. TNX_QR_CLUSTER=8 or 16 restricts the cluster size and TNX_QR_PANEL=fp64 keeps
+// FP64 panels in the FP64-class modes (tuning).
 struct PanelPlan {
   int nb, cl;
+  bool df;
 };
 
-template <int NB, int CL>
+template <int NB, int CL, bool DF>
 bool panel_fits(int64_t m) {
-  const PanelKernelInfo& info = panel_info<NB, CL>();
+  const PanelKernelInfo& info = panel_info<NB, CL, DF>();
   const int64_t rpc = (m + CL - 1) / CL;
-  return info.ok && size_t(NB + 2) * panel_ld(rpc, PT / NB) * sizeof(double) <= info.max_dyn;
+  return info.ok && size_t(NB + 2) * panel_ld(rpc, panel_threads<DF>() / NB) * sizeof(double) <= info.max_dyn;
 }
 
-PanelPlan plan_panels(int64_t m) {
+PanelPlan plan_panels(int64_t m, bool df) {
   static const int only = [] {
     const char* e = getenv("TNX_QR_CLUSTER");
     return e ? atoi(e) : 0;
   }();
+  static const bool fp64_panels = [] {
+    const char* e = getenv("TNX_QR_PANEL");
+    return e && std::string(e) == "fp64";
+  }();
   const bool c8 = only == 0 || only == 8, c16 = only == 0 || only == 16;
-  if (c16 && panel_fits<64, 16>(m)) return {64, 16};
-  if (c8 && panel_fits<64, 8>(m)) return {64, 8};
-  if (c16 && panel_fits<32, 16>(m)) return {32, 16};
-  if (c8 && panel_fits<32, 8>(m)) return {32, 8};
-  return {QB, 0};
+  if (df && !fp64_panels) {
+    if (c16 && panel_fits<64, 16, true>(m)) return {64, 16, true};
+    if (c8 && panel_fits<64, 8, true>(m)) return {64, 8, true};
+  }
+  if (c16 && panel_fits<64, 16, false>(m)) return {64, 16, false};
+  if (c8 && panel_fits<64, 8, false>(m)) return {64, 8, false};
+  if (c16 && panel_fits<32, 16, false>(m)) return {32, 16, false};
+  if (c8 && panel_fits<32, 8, false>(m)) return {32, 8, false};
+  return {QB, 0, false};
 }
 
 int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, double* tau, double* T,
@@ -573,10 +597,15 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
   if (pp.cl == 0) {
     panel_kernel<<<1, QT, 0, st>>>(F, m, j0, nb, tau, T);
     TNX_LAUNCH_CHECK();
+  } else if (pp.df) {
+    rc = pp.cl == 16 ? launch_panel<64, 16, true>(F, m, j0, nb, tau, T, st)
+                     : launch_panel<64, 8, true>(F, m, j0, nb, tau, T, st);
   } else if (pp.nb == 64) {
-    rc = pp.cl == 16 ? launch_panel<64, 16>(F, m, j0, nb, tau, T, st) : launch_panel<64, 8>(F, m, j0, nb, tau, T, st);
+    rc = pp.cl == 16 ? launch_panel<64, 16, false>(F, m, j0, nb, tau, T, st)
+                     : launch_panel<64, 8, false>(F, m, j0, nb, tau, T, st);
   } else {
-    rc = pp.cl == 16 ? launch_panel<32, 16>(F, m, j0, nb, tau, T, st) : launch_panel<32, 8>(F, m, j0, nb, tau, T, st);
+    rc = pp.cl == 16 ? launch_panel<32, 16, false>(F, m, j0, nb, tau, T, st)
+                     : launch_panel<32, 8, false>(F, m, j0, nb, tau, T, st);
   }
   profile_mark(KF_QR_PANEL, st, false);
   return rc;
@@ -630,7 +659,7 @@ int look_ahead(LookAhead** out) {
 // the rest of the GPU idle. Panel p+2's columns (part of that bulk) are used only after the
 // look-ahead stream's update of step p has completed. V is double-buffered between the streams.
 int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false) {
-  const PanelPlan pp = plan_panels(m);
+  const PanelPlan pp = plan_panels(m, df);
   const int NB = pp.nb;
   const int64_t np = (n + NB - 1) / NB;
   LookAhead* la = nullptr;
