@@ -10,6 +10,9 @@
 // Tiling: 64 x 128 output tile per CTA, 16-deep K slab, 256 threads, 4 x 8 outputs per
 // thread at stride 16 (conflict-free shared-memory reads), operands staged as float pairs;
 // the next slab's global loads are issued into registers before the current slab's products.
+// One such tile is ~0.5M double-FP32 products, tens of microseconds on one SM: products whose
+// large-tile grid would not fill two waves of the GPU (the narrow QR panel updates, small
+// split-K slices) use 32 x 32 tiles of 64 threads instead, eight times as many CTAs.
 #include <cuda_runtime.h>
 
 #include "tnx_internal.cuh"
@@ -17,8 +20,7 @@
 namespace tnx {
 namespace {
 
-constexpr int DM = 64, DN = 128, DK = 16, DT = 256;
-constexpr int RI = DM / 16, RJ = DN / 16;  // outputs per thread
+constexpr int DK = 16;
 
 __device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, float& ch, float& cl) {
   const float p = ah * bh;
@@ -32,12 +34,18 @@ __device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, f
   cl += err + e;
 }
 
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int64_t K, double alpha,
+// BM x BN output tile, NT threads: thread (tx, ty) = (tid % 16, tid / 16) owns rows ty + TY i
+// and columns tx + 16 j
+template <bool TA, bool TB, int BM, int BN, int NT>
+__global__ void __launch_bounds__(NT) gemm_df64_kernel(int64_t M, int64_t N, int64_t K, double alpha,
                                                      const double* __restrict__ A, int64_t lda, int64_t sa,
                                                      const double* __restrict__ B, int64_t ldb, int64_t sb,
                                                      double beta, double* __restrict__ C, int64_t ldc, int64_t sc,
                                                      int64_t k_total) {
+  constexpr int DM = BM, DN = BN, DT = NT, TY = NT / 16;
+  constexpr int RI = DM / TY, RJ = DN / 16;  // outputs per thread
+  static_assert(NT % 16 == 0 && DM % TY == 0 && DN % 16 == 0 && (DM * DK) % NT == 0 && (DN * DK) % NT == 0,
+                "df64 GEMM tile");
   __shared__ float Ah[DK][DM + 4], Al[DK][DM + 4];
   __shared__ float Bh[DK][DN + 4], Bl[DK][DN + 4];
   const int64_t bz = blockIdx.z;
@@ -102,8 +110,8 @@ __global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int
       float ah[RI], al[RI], bh[RJ], bl[RJ];
 #pragma unroll
       for (int i = 0; i < RI; ++i) {
-        ah[i] = Ah[kk][ty + 16 * i];
-        al[i] = Al[kk][ty + 16 * i];
+        ah[i] = Ah[kk][ty + TY * i];
+        al[i] = Al[kk][ty + TY * i];
       }
 #pragma unroll
       for (int j = 0; j < RJ; ++j) {
@@ -123,7 +131,7 @@ __global__ void __launch_bounds__(DT) gemm_df64_kernel(int64_t M, int64_t N, int
   }
 #pragma unroll
   for (int i = 0; i < RI; ++i) {
-    const int64_t gm = m0 + ty + 16 * i;
+    const int64_t gm = m0 + ty + TY * i;
     if (gm >= M) continue;
 #pragma unroll
     for (int j = 0; j < RJ; ++j) {
@@ -144,17 +152,24 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
   if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
   if (k <= 0) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st);
   TNX_CHECK_SHAPE(batch <= 65535, "gemm_df64: batch %lld > 65535", (long long)batch);
-  dim3 grid((unsigned)((n + DN - 1) / DN), (unsigned)((m + DM - 1) / DM), (unsigned)batch);
+  const int64_t big = ((n + 127) / 128) * ((m + 63) / 64) * batch;
+  const bool small = big < 2 * 152;
+  const int64_t bm = small ? 32 : 64, bn = small ? 32 : 128;
+  dim3 grid((unsigned)((n + bn - 1) / bn), (unsigned)((m + bm - 1) / bm), (unsigned)batch);
   TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_df64: m too large");
   profile_mark(KF_F64_GEMM, st, true);
-  if (!ta && !tb)
-    gemm_df64_kernel<false, false><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
-  else if (ta && !tb)
-    gemm_df64_kernel<true, false><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
-  else if (!ta && tb)
-    gemm_df64_kernel<false, true><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
-  else
-    gemm_df64_kernel<true, true><<<grid, DT, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+  auto go = [&](auto kernel, int nt) { kernel<<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total); };
+  if (small) {
+    if (!ta && !tb) go(gemm_df64_kernel<false, false, 32, 32, 64>, 64);
+    else if (ta && !tb) go(gemm_df64_kernel<true, false, 32, 32, 64>, 64);
+    else if (!ta && tb) go(gemm_df64_kernel<false, true, 32, 32, 64>, 64);
+    else go(gemm_df64_kernel<true, true, 32, 32, 64>, 64);
+  } else {
+    if (!ta && !tb) go(gemm_df64_kernel<false, false, 64, 128, 256>, 256);
+    else if (ta && !tb) go(gemm_df64_kernel<true, false, 64, 128, 256>, 256);
+    else if (!ta && tb) go(gemm_df64_kernel<false, true, 64, 128, 256>, 256);
+    else go(gemm_df64_kernel<true, true, 64, 128, 256>, 256);
+  }
   profile_mark(KF_F64_GEMM, st, false);
   profile_work(KF_F64_GEMM, 2.0 * double(m) * n * (k_total > 0 ? k_total : k * batch),
                8.0 * (double(m) * k + double(k) * n + double(m) * n) * batch);

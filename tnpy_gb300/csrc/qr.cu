@@ -438,6 +438,15 @@ inline int qr_nsplit(int64_t k) {
   int64_t s = (k + 127) / 128;
   return int(s < 1 ? 1 : (s > QR_SPLIT_MAX ? QR_SPLIT_MAX : s));
 }
+// K split of an m x n product with a long K into slices of >= 64 for up to `cap` partial
+// doubles: narrow products (the next panel's update) get more, shorter slices
+inline int qr_nsplit_cap(int64_t k, int64_t m, int64_t n, int64_t cap) {
+  int64_t s = (k + 63) / 64;
+  const int64_t c = cap / (m * n);
+  if (s > c) s = c;
+  if (s > 64) s = 64;
+  return int(s < 1 ? 1 : s);
+}
 
 // sized for QBMAX-wide panels, which also covers QB-wide ones
 size_t qr_layout(int64_t m, int64_t n, void* base, QrWs* w) {
@@ -614,11 +623,12 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
 // C -= V T^T V^T C for the mp x nc column-major block C (ld m): the trailing update of one
 // panel (V: mp x nb column-major in Vp, T: column-major ld NB)
 int apply_panel_t(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int64_t nc,
-                  double* W1, double* W2, double* part, cudaStream_t st, bool df) {
+                  double* W1, double* W2, double* part, int64_t part_cap, cudaStream_t st, bool df) {
   if (nc <= 0) return TNX_OK;
   // Row-major views: C (column-major mp x nc, ld m) is C^T (nc x mp, ld m), V is V^T (nb x mp).
-  // W1 (nb x nc) = V^T C  (short output rows, long K: split over K)
-  TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, Vp, mp, C, m, 0.0, W1, nc, qr_nsplit(mp), part, st, df));
+  // W1 (nb x nc) = V^T C  (short output rows, long K: split over K; finer for narrow C)
+  const int ns = nc <= NB ? qr_nsplit_cap(mp, nb, nc, part_cap) : qr_nsplit(mp);
+  TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, Vp, mp, C, m, 0.0, W1, nc, ns, part, st, df));
   // W2 = T^T W1   (T column-major with ld NB is T^T row-major)
   TNX_TRY(gemm_fp64_class(df, false, false, nb, nc, nb, 1.0, Tp, NB, 0, W1, nc, 0, 0.0, W2, nc, 0, 1, st));
   // C -= V W2, i.e. C^T -= W2^T V^T
@@ -662,6 +672,7 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
   const PanelPlan pp = plan_panels(m, df);
   const int NB = pp.nb;
   const int64_t np = (n + NB - 1) / NB;
+  const int64_t part_cap = int64_t(QR_SPLIT_MAX) * n * QBMAX;  // doubles of each split-K scratch
   LookAhead* la = nullptr;
   TNX_TRY(look_ahead(&la));
   // the look-ahead stream starts after everything queued on the caller's stream
@@ -683,9 +694,10 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
     if (rest > 0) {
       TNX_CUDA(cudaEventRecord(la->ev_v, st));  // V_p, T_p ready; panel p+2's columns updated by H_{p-1}
       TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_v, 0));
-      TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, la->aux, df));
+      TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, part_cap,
+                            la->aux, df));
     }
-    TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, st, df));
+    TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, st, df));
     TNX_TRY(factor_panel(pp, w.F, m, j0 + nb, nb1, w.tau + (p + 1) * NB, w.T + (p + 1) * NB * NB, st));
     if (rest > 0) {
       // the next step reads panel p+2's columns and rewrites the other V buffer
