@@ -111,15 +111,21 @@ int tnx_env_update(int direction, const double* E_in, const double* A, const dou
  * x: in = start vector (need not be normalised), out = unit Ritz vector.
  * Stops when ||H x - theta x|| <= tol * max(1, |theta|) (primme's residual criterion relative to
  * the operator scale), or after max_iter matvecs (TNX_ERR_NOT_CONVERGED, best Ritz pair still
- * written). precision selects the matvec; reorthogonalisation,
- * Rayleigh-Ritz and the final residual are FP64. With TNX_BF16X3 the returned energy and
- * residual are recomputed with one FP64 matvec (defect correction). */
+ * written). precision selects the matvec; Rayleigh-Ritz is FP64. With TNX_BF16X3 a first phase
+ * runs split-BF16 matvecs on FP32 vectors to a residual of ~3e-6 |theta|; an anchored phase
+ * then continues from the Ritz vector x with one FP64-class product H x per anchor (exact
+ * first row of the projected matrix, split-BF16 products for the corrections) until the
+ * FP64-class residual is below max(tol, 2e-7) |theta|. */
 size_t tnx_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
                                      int64_t dr, int max_basis, int precision);
 int tnx_davidson1(const double* L, const double* W, const double* R, double* x, int64_t chi_l,
                   int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter,
                   int max_basis, int precision, double* eval_out, double* resid_out,
                   int* iters_out, void* workspace, size_t workspace_bytes, void* stream);
+/* Counters of the calling host thread's last tnx_davidson1 call: out[0] matvecs of the first
+ * phase, out[1] matvecs of the anchored phase (TNX_BF16X3; 0 otherwise), out[2] FP64-class
+ * anchor products, out[3] thick restarts. */
+int tnx_davidson1_stats(int* out);
 
 /* ---- dense symmetric eigensolver (batched, one CTA per matrix) ---------------------------
  * Replaces linalg.eigh (tnpy/linalg.py:42-61) and the np.linalg.eigh of

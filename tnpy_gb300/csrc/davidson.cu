@@ -290,6 +290,12 @@ int dots(const T* V, int64_t ldv, int k, const T* w, int64_t n, double* part, do
 
 }  // namespace
 
+// Counters of the calling thread's last davidson1 call (tnx_davidson1_stats)
+struct DavStats {
+  int phase1 = 0, anchored = 0, anchors = 0, restarts = 0;
+};
+thread_local DavStats g_dav_stats;
+
 // Davidson driver. All pointers device; eval/resid/iters host.
 int davidson1(const double* L, const double* W, const double* R, double* x_io, int64_t chi_l, int64_t d,
               int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter, int mb, int precision,
@@ -437,6 +443,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   };
 
   bool converged = false;
+  int restarts = 0, anchors = 0, phase1 = 0;
   // Stagnation: the split-BF16 operand is not exactly symmetric, so the residual of the
   // mixed operator stops falling at ~1e-5 |H| (its rounding floor); the first phase ends when
   // the residual has not improved by 10% within `patience` matvecs. The FP64 form uses a longer
@@ -449,7 +456,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // solve on an excited state), and then converges the FP64-class residual to
   // max(tol, 2e-7) |theta|: the energy error is quadratic in the residual,
   // ~ (2e-7 |theta|)^2 / gap, i.e. below 1e-12 |E| for local gaps above 1e-2.
-  const double mixed_handover = 3e-6, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
+  const double mixed_handover = 3e-6, mixed_near_floor = 1e-4, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
   for (;;) {
     bool fell_in = false;
     TNX_TRY(f32 ? expand(v32, false, &fell_in) : expand(v64, false, &fell_in));
@@ -477,6 +484,13 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       converged = true;
       break;
     }
+    // A start vector already within ~10x of the split-BF16 residual floor (the usual case
+    // once the sweeps have converged) gains nothing from the first phase, which would only
+    // stagnate there: hand over at once.
+    if (mixed && k == 1 && rnorm <= mixed_near_floor * fmax(1.0, fabs(theta))) {
+      converged = true;
+      break;
+    }
     if (rnorm < 0.9 * best) {
       best = rnorm;
       best_it = iters;
@@ -486,8 +500,12 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     }
     if (iters >= max_iter) break;
     precond = 1;
-    if (k == mb) TNX_TRY(f32 ? restart(v32) : restart(v64));
+    if (k == mb) {
+      TNX_TRY(f32 ? restart(v32) : restart(v64));
+      ++restarts;
+    }
   }
+  phase1 = iters;
   if (mixed) {
     // Anchored phase. One double-FP32 matvec gives AV[0] = H x exactly for the current Ritz
     // vector x = V[0]; the Davidson then continues with split-BF16 products for the new
@@ -523,6 +541,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       TNX_LAUNCH_CHECK();
       TNX_TRY(matvec1_f64(L, W, R, w.V, w.AV, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, /*df=*/true, w.oz,
                           w.oz_bytes));
+      ++anchors;
       TNX_TRY(dots(w.V, n, 1, w.AV, n, w.part, w.Hm, 1, nullptr, 0, st));
       k = 1;
       precond = 1;
@@ -565,6 +584,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
         if (k == mb) {
           drift += sqrt(fmax(1.0 - c0 * c0, 0.0));
           TNX_TRY(restart(v64));
+          ++restarts;
         }
       }
       if (converged || iters >= max_iter) break;
@@ -575,6 +595,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   if (eval_out) *eval_out = theta;
   if (resid_out) *resid_out = rnorm;
   if (iters_out) *iters_out = iters;
+  g_dav_stats = {phase1, iters - phase1, anchors, restarts};
   if (!converged) {
     set_error("tnx_davidson1: %d matvecs, residual %.3e > tol %.3e", iters, rnorm,
               mixed ? mixed_rtol * fmax(1.0, fabs(theta)) : tol);
@@ -593,6 +614,15 @@ size_t tnx_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, in
                                      int max_basis, int precision) {
   if (max_basis > MAXB) max_basis = MAXB;
   return dav_layout(chi_l, d, chi_r, dl, dr, max_basis, precision, nullptr, 0, nullptr);
+}
+
+int tnx_davidson1_stats(int* out) {
+  TNX_CHECK_ARG(out, "null pointer");
+  out[0] = g_dav_stats.phase1;
+  out[1] = g_dav_stats.anchored;
+  out[2] = g_dav_stats.anchors;
+  out[3] = g_dav_stats.restarts;
+  return TNX_OK;
 }
 
 int tnx_davidson1(const double* L, const double* W, const double* R, double* x, int64_t chi_l, int64_t d,

@@ -124,6 +124,14 @@ def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64"
     return ev.value, rn.value, it.value, converged
 
 
+def davidson1_stats() -> dict:
+    """Counters of this thread's last davidson1 call: first-phase matvecs, anchored-phase
+    matvecs (mixed form), FP64-class anchor products and thick restarts."""
+    out = (ctypes.c_int * 4)()
+    check("tnx_davidson1_stats", lib.tnx_davidson1_stats(out))
+    return {"phase1": out[0], "anchored": out[1], "anchors": out[2], "restarts": out[3]}
+
+
 def eigh_batched(mats: list[torch.Tensor], keep: int):
     """Lowest `keep` eigenpairs of each symmetric matrix (one CTA per matrix).
 
