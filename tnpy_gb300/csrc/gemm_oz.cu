@@ -2,16 +2,19 @@
 //
 //   C = alpha op(A) op(B) + beta C,   FP64 in and out.
 //
-// Row i of op(A) is scaled by 2^-ea_i so that its entries are below 1 in magnitude and cut, by
-// integer extraction from the 53-bit mantissa in fixed point, into S = 8 slices of 7 bits:
-//   op(A)_ik 2^-ea_i = sum_{s<S} qa_s,ik 2^-7(s+1) + r_ik,   |r_ik| < 2^-56,   |qa_s,ik| <= 127,
+// Row i of op(A) is scaled by 2^-ea_i so that its entries are below 1/2 in magnitude and cut, by
+// integer extraction from the 53-bit mantissa in signed fixed point, into S = 8 balanced base-128
+// digits (each rounded to nearest, so the remainder after digit s is at most half a unit of it):
+//   op(A)_ik 2^-ea_i = sum_{s<S} qa_s,ik 2^-7(s+1) + r_ik,   |r_ik| <= 2^-57,   |qa_s,ik| <= 64,
 // integers that BF16 holds exactly. Column j of op(B) likewise with eb_j. Then
-//   C_ij = 2^(ea_i + eb_j) sum_{g<S} 2^-7(g+2) P_g,ij + O(2^-52) per product,
+//   C_ij = 2^(ea_i + eb_j) sum_{g<S} 2^-7(g+2) P_g,ij + O(2^-53) per product,
 //   P_g,ij = sum_{s+t=g} sum_k qa_s,ik qb_t,kj                          (36 slice pairs),
-// and every P_g is a sum of integer products below 2^14. Over KC = 128 values of k the partial
-// sum of a group (at most 8 pairs) stays below 8 * 128 * 127^2 < 2^24, so the FP32 accumulation
-// of the tensor cores in tensor memory is exact; every KC the eight group accumulators are
-// drained into a double-FP32 running sum per output (epilogue warps), scaled by 2^-7(g+2).
+// and every P_g is a sum of integer products of magnitude at most 2^12. Over KC = 480 values of
+// k the partial sum of a group (at most 8 pairs) stays below 8 * 480 * 2^12 < 2^24, so the FP32
+// accumulation of the tensor cores in tensor memory is exact; every KC the eight group
+// accumulators are drained into a double-FP32 running sum per output (epilogue warps), scaled
+// by 2^-7(g+2). (Unbalanced 7-bit digits up to 127 would allow only KC = 128: the drains, which
+// stall the MMAs, are 3.75x rarer with balanced ones.)
 // Error: ~2^-52 per product relative to 2^ea_i 2^eb_j (the row / column maxima), plus the
 // double-FP32 summation (~2^-46 of the running sum): FP64-class where rows and columns do not
 // span many decades; at the tensor cores' rate divided by 36.
@@ -37,14 +40,14 @@ using namespace tc;
 
 constexpr int OZ_S = 8;                         // slices per operand
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;  // BK = 32 bf16 = one 64-byte swizzle row
-constexpr int OZ_KC = 128;                      // K values per exact accumulation chunk
+constexpr int OZ_KC = 480;                      // K values per exact accumulation chunk
 constexpr int OZ_STAGES = 2;                    // a stage holds all 2 S slice tiles of one K block
 constexpr int OZ_THREADS = 192;
 constexpr uint32_t OZ_TMEM_COLS = 512;
 
 // ---------------------------------------------------------------- operand slicing
 // Logical operand X(r, k) = src[r * rs + k * ks], rows x K (FP64). exps[r] = row scale exponent
-// E (|X(r, k)| < 2^E for all k; 0 for an all-zero row). One CTA (32 x 8 threads) per 32 rows.
+// E (|X(r, k)| < 2^(E-1) for all k; 0 for an all-zero row). One CTA (32 x 8 threads) per 32 rows.
 __global__ void oz_rowexp_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
                                  int* __restrict__ exps, int64_t rows_pad) {
   __shared__ int tile[32][33];
@@ -65,10 +68,10 @@ __global__ void oz_rowexp_kernel(const double* __restrict__ src, int64_t rows, i
       for (int j = 0; j < 32; ++j) best = max(best, tile[tx][j]);
     __syncthreads();
   }
-  if (ty == 0 && r0 + tx < rows_pad) exps[r0 + tx] = (best > 0 && r0 + tx < rows) ? best - 1022 : 0;
+  if (ty == 0 && r0 + tx < rows_pad) exps[r0 + tx] = (best > 0 && r0 + tx < rows) ? best - 1021 : 0;
 }
 
-// bf16 bit pattern of an integer 0 <= q <= 127 (exact)
+// bf16 bit pattern of an integer 0 <= q <= 255 (exact)
 __device__ __forceinline__ uint16_t bf16_of_small_int(unsigned q, unsigned sign) {
   if (q == 0u) return 0;
   const int e = 31 - __clz(q);
@@ -95,18 +98,22 @@ __global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, in
     const int64_t r = r0 + i, k = k0 + tx;
     if (r >= rows_pad || k >= Kp) continue;
     const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(tile[i][tx]));
-    const unsigned sign = unsigned(u >> 63);
     const int eb = int((u >> 52) & 0x7ffu);
-    unsigned long long F = 0;  // |x| 2^-E in fixed point with 63 fraction bits
+    long long X = 0;  // x 2^-E in signed fixed point with 63 fraction bits, |X| < 2^62
     if (eb != 0 && r < rows) {
       const unsigned long long m53 = (u & ((1ull << 52) - 1)) | (1ull << 52);
-      const int shift = eb - 1012 - exps[r];  // <= 10 since |x| < 2^E
-      F = shift >= 0 ? (m53 << shift) : (-shift < 64 ? (m53 >> -shift) : 0ull);
+      const int shift = eb - 1012 - exps[r];  // <= 9 since |x| < 2^(E-1)
+      const unsigned long long F = shift >= 0 ? (m53 << shift) : (-shift < 64 ? (m53 >> -shift) : 0ull);
+      X = (u >> 63) ? -static_cast<long long>(F) : static_cast<long long>(F);
     }
+    // balanced digits: q_s = X / 2^(56 - 7s) rounded to nearest, X -= q_s 2^(56 - 7s); the
+    // remainder before digit s is at most 2^(62 - 7s) in magnitude, so |q_s| <= 64
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) {
-      const unsigned q = unsigned(F >> (63 - 7 * (s + 1))) & 0x7fu;
-      planes[(size_t(s) * rows_pad + r) * Kp + k] = bf16_of_small_int(q, sign);
+      const int sh = 56 - 7 * s;
+      const long long q = (X + (1LL << (sh - 1))) >> sh;
+      X -= q * (1LL << sh);
+      planes[(size_t(s) * rows_pad + r) * Kp + k] = bf16_of_small_int(unsigned(q < 0 ? -q : q), q < 0 ? 1u : 0u);
     }
   }
 }
