@@ -15,6 +15,8 @@
 // split-K slices) use 32 x 32 tiles of 64 threads instead, eight times as many CTAs.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "tnx_internal.cuh"
 
 namespace tnx {
@@ -152,8 +154,13 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
   if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
   if (k <= 0) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st);
   TNX_CHECK_SHAPE(batch <= 65535, "gemm_df64: batch %lld > 65535", (long long)batch);
+  // TNX_DF64_SMALL_WAVES (tuning, default 2): large-tile waves below which 32 x 32 tiles are used
+  static const int small_waves = [] {
+    const char* e = getenv("TNX_DF64_SMALL_WAVES");
+    return e ? atoi(e) : 2;
+  }();
   const int64_t big = ((n + 127) / 128) * ((m + 63) / 64) * batch;
-  const bool small = big < 2 * 152;
+  const bool small = big < int64_t(small_waves) * 152;
   const int64_t bm = small ? 32 : 64, bn = small ? 32 : 128;
   dim3 grid((unsigned)((n + bn - 1) / bn), (unsigned)((m + bm - 1) / bm), (unsigned)batch);
   TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_df64: m too large");

@@ -46,15 +46,18 @@ constexpr int OZ_THREADS = 192;
 constexpr uint32_t OZ_TMEM_COLS = 512;
 
 // ---------------------------------------------------------------- operand slicing
-// Logical operand X(r, k) = src[r * rs + k * ks], rows x K (FP64). exps[r] = row scale exponent
-// E (|X(r, k)| < 2^(E-1) for all k; 0 for an all-zero row). One CTA (32 x 8 threads) per 32 rows.
-__global__ void oz_rowexp_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
-                                 int* __restrict__ exps, int64_t rows_pad) {
+// Logical operand X(r, k) = src[r * rs + k * ks], rows x K (FP64). bmax[r] (zeroed before) =
+// largest biased FP64 exponent in row r, by atomicMax over CTAs of 32 rows x OZ_SCAN_K values of
+// k (the scan runs over the whole grid, not one CTA per row block). The row's scale exponent is
+// E = bmax - 1021 (|X(r, k)| < 2^(E-1)), 0 for an all-zero row: row_scale_exp.
+constexpr int OZ_SCAN_K = 256;
+__global__ void oz_rowmax_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
+                                 int* __restrict__ bmax) {
   __shared__ int tile[32][33];
-  const int64_t r0 = int64_t(blockIdx.x) * 32;
+  const int64_t r0 = int64_t(blockIdx.y) * 32, kb = int64_t(blockIdx.x) * OZ_SCAN_K;
   const int tx = threadIdx.x, ty = threadIdx.y;
   int best = 0;  // biased exponent, 0 = zero / denormal
-  for (int64_t k0 = 0; k0 < K; k0 += 32) {
+  for (int64_t k0 = kb; k0 < K && k0 < kb + OZ_SCAN_K; k0 += 32) {
     for (int i = ty; i < 32; i += 8) {
       // unit stride along k: tx runs over k; along r: tx runs over r
       const int64_t r = ks == 1 ? r0 + i : r0 + tx, k = ks == 1 ? k0 + tx : k0 + i;
@@ -68,8 +71,10 @@ __global__ void oz_rowexp_kernel(const double* __restrict__ src, int64_t rows, i
       for (int j = 0; j < 32; ++j) best = max(best, tile[tx][j]);
     __syncthreads();
   }
-  if (ty == 0 && r0 + tx < rows_pad) exps[r0 + tx] = (best > 0 && r0 + tx < rows) ? best - 1021 : 0;
+  if (ty == 0 && best > 0 && r0 + tx < rows) atomicMax(&bmax[r0 + tx], best);
 }
+
+__device__ __forceinline__ int row_scale_exp(int bmax) { return bmax > 0 ? bmax - 1021 : 0; }
 
 // bf16 bit pattern of an integer 0 <= q <= 255 (exact)
 __device__ __forceinline__ uint16_t bf16_of_small_int(unsigned q, unsigned sign) {
@@ -79,7 +84,7 @@ __device__ __forceinline__ uint16_t bf16_of_small_int(unsigned q, unsigned sign)
   return uint16_t((sign << 15) | (unsigned(127 + e) << 7) | mant);
 }
 
-// planes[s][r][k] (row pitch Kp, rows_pad rows per plane) = slice s of X(r, k) 2^-exps[r];
+// planes[s][r][k] (row pitch Kp, rows_pad rows per plane) = slice s of X(r, k) 2^-E[r];
 // zero for r >= rows or k >= K.
 __global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
                                 const int* __restrict__ exps, uint16_t* __restrict__ planes, int64_t rows_pad,
@@ -102,7 +107,7 @@ __global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, in
     long long X = 0;  // x 2^-E in signed fixed point with 63 fraction bits, |X| < 2^62
     if (eb != 0 && r < rows) {
       const unsigned long long m53 = (u & ((1ull << 52) - 1)) | (1ull << 52);
-      const int shift = eb - 1012 - exps[r];  // <= 9 since |x| < 2^(E-1)
+      const int shift = eb - 1012 - row_scale_exp(exps[r]);  // <= 9 since |x| < 2^(E-1)
       const unsigned long long F = shift >= 0 ? (m53 << shift) : (-shift < 64 ? (m53 >> -shift) : 0ull);
       X = (u >> 63) ? -static_cast<long long>(F) : static_cast<long long>(F);
     }
@@ -264,12 +269,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&chunk_empty)) : "memory");
     }
     if (ok && row < M) {
-      const int er = ea[row];
+      const int er = row_scale_exp(ea[row]);
       double* o = C + int64_t(row) * ldc + n0;
 #pragma unroll
       for (int j = 0; j < OZ_BN; ++j) {
         if (n0 + j < N) {
-          double v = ldexp(join_df(hi[j], lo[j]), er + eb[n0 + j]);
+          double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
           v *= alpha;
           if (beta != 0.0) v = fma(beta, o[j], v);
           o[j] = v;
@@ -334,9 +339,12 @@ int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, con
   const int64_t a_rs = ta ? 1 : lda, a_ks = ta ? lda : 1;
   const int64_t b_rs = tb ? ldb : 1, b_ks = tb ? 1 : ldb;
   dim3 tb2(32, 8);
-  oz_rowexp_kernel<<<unsigned(L.Mp / 32), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea, L.Mp);
+  // row maxima (atomicMax into zeroed arrays) and the error flag: ea, eb and flag are consecutive
+  TNX_CUDA(cudaMemsetAsync(L.ea, 0, reinterpret_cast<char*>(L.flag + 1) - reinterpret_cast<char*>(L.ea), st));
+  const unsigned kscan = unsigned((k + OZ_SCAN_K - 1) / OZ_SCAN_K);
+  oz_rowmax_kernel<<<dim3(kscan, unsigned(L.Mp / 32)), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea);
   TNX_LAUNCH_CHECK();
-  oz_rowexp_kernel<<<unsigned(L.Np / 32), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb, L.Np);
+  oz_rowmax_kernel<<<dim3(kscan, unsigned(L.Np / 32)), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb);
   TNX_LAUNCH_CHECK();
   oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Mp / 32)), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea, L.sa,
                                                                                   L.Mp, L.Kp);
@@ -353,7 +361,6 @@ int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, con
     TNX_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     attr.store(true);
   }
-  TNX_CUDA(cudaMemsetAsync(L.flag, 0, sizeof(int), st));
   dim3 grid(unsigned(L.Np / OZ_BN), unsigned(L.Mp / OZ_BM));
   profile_mark(KF_OZ_GEMM, st, true);
   oz_gemm_kernel<<<grid, OZ_THREADS, smem, st>>>(ma, mb, int(m), int(n), int(L.Kp), int(L.Mp), int(L.Np), L.ea, L.eb,
