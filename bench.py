@@ -106,9 +106,9 @@ def cpu_sample(a, matvecs_per_site: float | None = None):
     """CPU restatement of the reference's per-site work at the bench's n and chi, timed on the
     host cores: one-site matvec (the primme callback), SVD gauge move (split_tensor) and
     environment update, each repeated for a bounded time at a middle site of the chain.
-    A site update costs (matvecs_per_site + 1) matvecs (Davidson + perturbation) + 1 split
-    + 1 environment update; a sweep is n-1 site updates. matvecs_per_site is the average
-    the GPU run needed (20 when not given)."""
+    A site update costs matvecs_per_site matvecs (the eigensolver) + 1 split + 1 environment
+    update; a sweep is n-1 site updates. matvecs_per_site is the FP64 GPU form's average on the
+    same state (20 when not given)."""
     import numpy as np
 
     from oracle import models as om
@@ -139,11 +139,11 @@ def cpu_sample(a, matvecs_per_site: float | None = None):
     t_split = timed(lambda: omps.split_tensor([x.copy(), nb.copy()], 0, rightward=True), 4.0)
     t_env = timed(lambda: omps.update_left(L, x, w), 4.0)
     mv = 20.0 if matvecs_per_site is None else float(matvecs_per_site)
-    per_site = (mv + 1.0) * t_mv + t_split + t_env
+    per_site = mv * t_mv + t_split + t_env
     return {"value": 1.0 / (per_site * (n - 1)), "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
             "sample": f"numpy/scipy FP64 restatement at site {site} of n={n}, chi={chi} (bonds {cl}x{cr}): "
                       f"matvec {t_mv * 1e3:.1f} ms, SVD split {t_split * 1e3:.1f} ms, env update "
-                      f"{t_env * 1e3:.1f} ms, each repeated for ~4 s; site update = ({mv:.1f}+1) matvecs + "
+                      f"{t_env * 1e3:.1f} ms, each repeated for ~4 s; site update = {mv:.2f} matvecs + "
                       f"split + env, {n - 1} site updates per sweep (full-chi site cost for every site)",
             "seconds_per_site": per_site, "matvecs_per_site": mv,
             "matvec_tflops": (40 * cl * cr * max(cl, cr) + 200 * cl * cr) / t_mv / 1e12}
@@ -186,6 +186,33 @@ def matvec_forms(f, site: int):
                      "s": time.perf_counter() - t0}
     out["local_eigensolve"] = evs
     out["local_dE_rel_mixed_vs_fp64"] = abs(evs["mixed"]["eval"] - evs["fp64"]["eval"]) / abs(evs["fp64"]["eval"])
+    return out
+
+
+def fp64_sweep(f, direction, tol: float, mixed_s: float):
+    """The plain FP64 GPU form against the mixed form on the same state: both chains start from a
+    copy of the bench chain's current MPS (environments rebuilt in each form) and sweep once in
+    the same direction; reports the FP64 sweep's seconds, the speed-up of the mixed form's timed
+    sweeps over it, and |dE|/|E| between the two energies after the sweep."""
+    import torch
+
+    import tnpy_gb300 as tg
+
+    out = {}
+    for form in ("fp64", "mixed"):
+        mps = tg.MatrixProductState([t.clone() for t in f.mps.tensors], device=f.mps.device)
+        g = tg.FiniteDMRG(f.env.mpo, bond_dim=f.bond_dim, mps=mps, precision=form, compute_variance=False,
+                          device=f.mps.device)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = g.sweep(direction, tol=tol)
+        torch.cuda.synchronize()
+        out[form] = {"s": time.perf_counter() - t0, "energy": e,
+                     "matvecs_per_site": g.stats["matvecs"] / max(1, g.stats["iterative_solves"])}
+        del g, mps
+        torch.cuda.empty_cache()
+    out["speedup_mixed_timed_vs_fp64"] = out["fp64"]["s"] / mixed_s
+    out["dE_rel_mixed_vs_fp64"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])
     return out
 
 
@@ -323,6 +350,7 @@ def run_ours(a):
     launches0 = lib.tnx_launch_count()
     lib.tnx_profile_begin(0)  # tcgen05 split-BF16 GEMM
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    mv0, it0 = f.stats["matvecs"], f.stats["iterative_solves"]
     ev0.record()
     t0 = time.perf_counter()
     for _ in range(a.steps):
@@ -331,6 +359,7 @@ def run_ours(a):
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
+    mv_timed = (f.stats["matvecs"] - mv0) / max(1, f.stats["iterative_solves"] - it0)
     launches = lib.tnx_launch_count() - launches0
     n_l, tot_ms, flops, nbytes = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
     lib.tnx_profile_end(ctypes.byref(n_l), ctypes.byref(tot_ms), ctypes.byref(flops), ctypes.byref(nbytes))
@@ -374,23 +403,45 @@ def run_ours(a):
             parts = ln.split()
             if len(parts) == 2 and not ln.startswith("#") and parts[0] == f"tc_gemm_chi{a.chi}":
                 traffic = float(parts[1])
-    roofline = {"kernel": "bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)",
+    roofline_mv = {"kernel": "bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)",
                 "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_note": "of measured: bf16_tflops_sustained / 3 (three BF16 products per split-BF16 product); "
                              "achieved counts algorithmic flops 2*M*N*K of the unsplit product",
                 "launches": n_l.value, "kernel_ms_total": tot_ms.value,
                 "share_of_step_time": (tot_ms.value / dev_ms) if dev_ms > 0 else None}
-    # FP64-class contractions on the tensor cores (Ozaki GEMM): one further sweep, outside the timed
-    # region, with CUDA events around each of its launches
-    lib.tnx_profile_begin(6)
-    one_sweep()
-    n_o, ms_o, fl_o, by_o = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
-    lib.tnx_profile_end(ctypes.byref(n_o), ctypes.byref(ms_o), ctypes.byref(fl_o), ctypes.byref(by_o))
+    # Kernel families: one further sweep per family, outside the timed region, with CUDA events
+    # around each launch of that family (library event profiler)
+    fams = ["tcgen05 split-BF16 GEMM", "double-FP32 GEMM (QR updates)", "Davidson vector kernels",
+            "QR panel (double-FP32 cluster kernel)", "eigh", "other", "Ozaki FP64-class GEMM"]
+    shares = {}
+    for fam in (6, 1, 3):
+        lib.tnx_profile_begin(fam)
+        sw0, sw1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sw0.record()
+        one_sweep()
+        sw1.record()
+        n_f, ms_f, fl_f, by_f = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+        lib.tnx_profile_end(ctypes.byref(n_f), ctypes.byref(ms_f), ctypes.byref(fl_f), ctypes.byref(by_f))
+        torch.cuda.synchronize()
+        shares[fams[fam]] = {"launches": n_f.value, "ms_per_sweep": ms_f.value,
+                             "share": ms_f.value / sw0.elapsed_time(sw1),
+                             "tflops": fl_f.value / (ms_f.value / 1e3) / 1e12 if ms_f.value > 0 and fl_f.value > 0
+                             else None}
+        if fam == 6:
+            n_o, ms_o, fl_o = n_f, ms_f, fl_f
+    shares[fams[0]] = {"launches": n_l.value, "ms_per_sweep": tot_ms.value / a.steps,
+                       "share": tot_ms.value / dev_ms if dev_ms > 0 else None, "tflops": achieved}
     oz_ach = fl_o.value / (ms_o.value / 1e3) / 1e12 if ms_o.value > 0 else None
     oz_peak = bf16_sust / 36.0
+    traffic_oz = None
+    if tf.exists():
+        for ln in tf.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) == 2 and not ln.startswith("#") and parts[0] == f"oz_gemm_chi{a.chi}":
+                traffic_oz = float(parts[1])
     roofline_oz = {"kernel": "oz_gemm_kernel (tcgen05 FP64-class GEMM, 36 exact BF16 slice products)",
-                   "bound": "tensor", "achieved": oz_ach, "peak": oz_peak, "unit": "TFLOP/s",
+                   "bound": "tensor", "achieved": oz_ach, "peak": oz_peak, "unit": "TFLOP/s", "traffic": traffic_oz,
                    "frac": (oz_ach / oz_peak) if oz_ach else None, "launches": n_o.value, "kernel_ms_per_sweep": ms_o.value,
                    "peak_note": "of measured: bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class "
                                 "product); achieved counts algorithmic flops 2*M*N*K"}
@@ -399,18 +450,21 @@ def run_ours(a):
             "vs_baseline": None, "dtype": "f64 (split-bf16 tensor-core matvec, FP64 environments / eigensolver)"
             if a.precision == "mixed" else "f64",
             "data": "synthetic (seeded random initial MPS, XXZ MPO)", "config": workload(a),
-            "roofline": roofline, "roofline_fp64_class": roofline_oz, "clocks": clk, "gpu_launches": int(launches),
+            "roofline": roofline_oz, "roofline_matvec": roofline_mv, "step_shares": shares, "clocks": clk,
+            "gpu_launches": int(launches),
             "e2e": {"value": world / e2e_t, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d + 8},
             "energy_last": energies[-1], "wall_s_per_step": wall / a.steps,
-            "davidson_matvecs_total": f.stats["matvecs"]}
-    sites_per_sweep = a.n - 1
-    mv_per_site = f.stats["matvecs"] / max(1, f.stats["iterative_solves"])
-    line["davidson_matvecs_per_site"] = mv_per_site
-    if rank == 0 and world == 1 and not a.no_cpu:
-        line["cpu_baseline"] = cpu_sample(a, mv_per_site)
+            "davidson_matvecs_per_site_timed": mv_timed}
+    # CPU restatement: per-site work scaled by the FP64 form's Davidson matvecs on the same state
+    # (the reference's primme call uses the same tol), else by the timed mixed count + the anchor
+    mv_cpu = mv_timed + 1.0
     if rank == 0 and not a.no_extras:
         line["matvec_forms"] = matvec_forms(f, a.n // 2)
+        line["fp64_sweep"] = fp64_sweep(f, dirs[step % 2], a.tol, t_step)
+        mv_cpu = line["fp64_sweep"]["fp64"]["matvecs_per_site"]
+    if rank == 0 and world == 1 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_sample(a, mv_cpu)
         line["tsdrg"] = tsdrg_rate(a.tsdrg_realizations, with_cpu=(world == 1 and not a.no_cpu))
         line["chains"] = chains_rate(a.chains, with_cpu=(world == 1 and not a.no_cpu))
     if rank == 0:
