@@ -102,13 +102,19 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ CPU sample (oracle)
+# Davidson matvecs per site of the FP64 GPU form on the timed sweeps' converged state (bench
+# field fp64_sweep.fp64.matvecs_per_site, measured 1.78 at n=100, chi=1024): the work per site of
+# the reference's primme call (same tol) where this run does not measure it (reference arm)
+REF_MATVECS_PER_SITE = 1.8
+
+
 def cpu_sample(a, matvecs_per_site: float | None = None):
     """CPU restatement of the reference's per-site work at the bench's n and chi, timed on the
     host cores: one-site matvec (the primme callback), SVD gauge move (split_tensor) and
     environment update, each repeated for a bounded time at a middle site of the chain.
     A site update costs matvecs_per_site matvecs (the eigensolver) + 1 split + 1 environment
     update; a sweep is n-1 site updates. matvecs_per_site is the FP64 GPU form's average on the
-    same state (20 when not given)."""
+    same state when measured in the same run, else REF_MATVECS_PER_SITE."""
     import numpy as np
 
     from oracle import models as om
@@ -138,7 +144,7 @@ def cpu_sample(a, matvecs_per_site: float | None = None):
     t_mv = timed(lambda: omps.one_site_matvec(L, w, R, x), 4.0)
     t_split = timed(lambda: omps.split_tensor([x.copy(), nb.copy()], 0, rightward=True), 4.0)
     t_env = timed(lambda: omps.update_left(L, x, w), 4.0)
-    mv = 20.0 if matvecs_per_site is None else float(matvecs_per_site)
+    mv = REF_MATVECS_PER_SITE if matvecs_per_site is None else float(matvecs_per_site)
     per_site = mv * t_mv + t_split + t_env
     return {"value": 1.0 / (per_site * (n - 1)), "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
             "sample": f"numpy/scipy FP64 restatement at site {site} of n={n}, chi={chi} (bonds {cl}x{cr}): "
