@@ -53,9 +53,13 @@ def test_davidson_mixed_defect_corrected(cuda, chi):
     L, W, R = env.left[site], om.uniform(mpo)[site], env.right[site]
     w = np.linalg.eigvalsh(omps.one_site_full_matrix(L, W, R))
     x64 = _t(m[site], cuda).clone()
-    e64, *_ = K.davidson1(_t(L, cuda), _t(W, cuda), _t(R, cuda), x64, tol=1e-10)
+    e64, _, its64, _ = K.davidson1(_t(L, cuda), _t(W, cuda), _t(R, cuda), x64, tol=1e-10)
+    st64 = K.davidson1_stats()
+    assert st64["phase1"] == its64 and st64["anchored"] == 0 and st64["anchors"] == 0, st64
     xm = _t(m[site], cuda).clone()
     em, rn, its, ok = K.davidson1(_t(L, cuda), _t(W, cuda), _t(R, cuda), xm, tol=1e-10, precision="mixed")
+    st = K.davidson1_stats()
+    assert st["phase1"] + st["anchored"] == its and st["anchors"] >= 1, st
     np.testing.assert_allclose(e64, w[0], rtol=1e-12)
     # the FP64 Rayleigh quotient of the mixed eigenvector: error quadratic in the vector error
     assert abs(em - w[0]) <= 1e-9 * abs(w[0]), (em, w[0], rn)

@@ -52,6 +52,16 @@ def test_workspace_queries_are_host_only(lib):
     assert g(64, 2, 64, 5, 5, 24, 0) > 2 * 24 * 64 * 2 * 64 * 8
 
 
+def test_davidson_stats_host_only(lib):
+    """The solver statistics are host-side, per thread: readable without a GPU."""
+    import tnpy_gb300._lib as L
+
+    out = (ctypes.c_int * 4)()
+    assert L.lib.tnx_davidson1_stats(out) == L.TNX_OK
+    assert all(v >= 0 for v in out)
+    assert L.lib.tnx_davidson1_stats(None) == L.TNX_ERR_INVALID_ARG
+
+
 def test_null_pointers_rejected_without_gpu(lib):
     import tnpy_gb300._lib as L
 
