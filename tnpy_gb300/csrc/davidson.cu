@@ -2,7 +2,8 @@
 // stays on the device, replacing linalg.eigshmv -> primme.eigsh(k=1, which='SA')
 // (tnpy/linalg.py:64-87) called from FiniteDMRG.one_site_solver (tnpy/finite_dmrg.py:97-111).
 //
-// Basis V (orthonormal, FP64) and AV = H V live in the caller's workspace; each expansion
+// Basis V (orthonormal; FP64, or FP32 in the mixed form's first phase) and AV = H V live in the
+// caller's workspace; each expansion
 //   1. orthogonalises the new direction against V (classical Gram-Schmidt, FP64, with a
 //      second pass when the first removed more than half of its norm: DGKS),
 //   2. applies H (FP64, double-FP32 or split-BF16 tensor-core matvec),
@@ -12,7 +13,9 @@
 //      direction t = r / (diag(H) - theta) (diagonal preconditioner).
 // The host loop reads three scalars per expansion to decide convergence. With the
 // split-BF16 matvec a second, anchored phase takes the residual from the split-BF16
-// floor to FP64-class accuracy: one double-FP32 matvec per anchor (see davidson1).
+// floor to FP64-class accuracy: one FP64-class matvec (tensor-core Ozaki GEMMs where large,
+// double-FP32 otherwise) per anchor; a start vector already near that floor goes to the
+// anchored phase after one matvec (see davidson1).
 #include <cuda_runtime.h>
 
 #include <cmath>

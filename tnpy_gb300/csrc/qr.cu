@@ -1,4 +1,5 @@
-// Householder QR (FP64) and the one-site gauge move of FiniteDMRG.sweep.
+// Householder QR (FP64, or FP64-class in double-FP32) and the one-site gauge move of
+// FiniteDMRG.sweep.
 //
 // Reference: linalg.qr (tnpy/linalg.py:26-39); the gauge move replaces the SVD split of
 // MatrixProductState.split_tensor (tnpy/matrix_product_state.py:187-225) as called through
@@ -9,9 +10,11 @@
 //
 // Blocked right-looking Householder on a column-major copy: each 64- (or 32-) column panel
 // is factored by one thread-block cluster holding the panel in shared memory (reflectors +
-// the compact-WY T factor; one-CTA kernel for panels too tall for a cluster), the trailing
-// matrix is updated with three FP64-class GEMMs (W = V^T C, W = T^T W, C -= V W), and Q is
-// formed by applying the panels backwards to [I; 0].
+// the compact-WY T factor; FP64 here, double-FP32 in qr_panel_df.cuh for the FP64-class
+// modes; one-CTA kernel for panels too tall for a cluster), the trailing matrix is updated
+// with three FP64 / double-FP32 GEMMs (W = V^T C, W = T^T W, C -= V W) with look-ahead (the
+// next panel's columns first, the rest on a second stream), and Q is formed by applying the
+// panels backwards to [I; 0].
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
