@@ -312,6 +312,19 @@ def run_reference(a):
 
 
 # ------------------------------------------------------------------ our arm
+def max_over_ranks(x: float, device) -> float:
+    """Largest x over the ranks of the default process group (x itself without one): the
+    whole-job step time is that of the slowest replica."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(a):
     import torch
     import torch.distributed as dist
@@ -370,11 +383,7 @@ def run_ours(a):
     n_l, tot_ms, flops, nbytes = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
     lib.tnx_profile_end(ctypes.byref(n_l), ctypes.byref(tot_ms), ctypes.byref(flops), ctypes.byref(nbytes))
     dev_ms = ev0.elapsed_time(ev1)
-    t_step = dev_ms / 1e3 / a.steps
-    if world > 1:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(dev_ms / 1e3 / a.steps, dev)
     value = world / t_step
 
     # ---- end-to-end: MPS round-trips through pinned host memory every step
@@ -392,11 +401,7 @@ def run_ours(a):
             h.copy_(t, non_blocking=True)
         torch.cuda.current_stream().synchronize()
     barrier()
-    e2e_t = (time.perf_counter() - t0) / a.steps
-    if world > 1:
-        tt = torch.tensor([e2e_t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t = max_over_ranks((time.perf_counter() - t0) / a.steps, dev)
 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     bf16_sust = peaks.get("bf16_tflops_sustained", 1700.0)
