@@ -38,10 +38,11 @@ enum tnx_status {
 enum tnx_precision {
   TNX_FP64 = 0,       /* plain FP64 contractions (FP64 pipe)                                */
   TNX_BF16X3 = 1,     /* mixed form: split-BF16 three-term matvec products on tcgen05 with FP32
-                         accumulation; environment updates, gauge moves and the defect-correction
-                         matvec in double-FP32 (TNX_DF64)                                       */
-  TNX_DF64 = 2        /* FP64-class contractions in double-FP32 arithmetic on the FP32 pipe
-                         (~2^-48 relative per product)                                          */
+                         accumulation for the Davidson iterations; environment updates, gauge
+                         moves and the Davidson's anchor matvec FP64-class as in TNX_DF64     */
+  TNX_DF64 = 2        /* FP64-class contractions: Ozaki-sliced FP64 GEMMs on tcgen05 where large
+                         (~2^-52 per product relative to row/column maxima), double-FP32 on the
+                         FP32 pipe otherwise (~2^-48 per product); double-FP32 QR panels       */
 };
 
 const char* tnx_status_string(int status);
