@@ -8,9 +8,10 @@ above), the 1e-5 perturbation psi += 1e-5 H_eff psi (:116-141), the gauge move
 onto the neighbour (QR form), and the environment update.
 
 ``precision='mixed'`` runs the Davidson matvecs as split-BF16 tensor-core
-contractions, recomputes each local energy with one FP64-class (double-FP32)
-matvec, and runs environment updates and gauge moves in double-FP32
-arithmetic; reorthogonalisation and Rayleigh-Ritz stay FP64.
+contractions and certifies each local eigenpair with FP64-class anchor matvecs
+(Ozaki-sliced FP64 GEMMs on the tensor cores), runs environment updates in the
+same FP64-class form and gauge moves with double-FP32 QR panels and updates;
+Rayleigh-Ritz stays FP64.
 """
 from __future__ import annotations
 
