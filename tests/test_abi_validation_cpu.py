@@ -1,0 +1,69 @@
+"""Error behaviour of the C ABI without a GPU: every entry point checks its arguments before it
+touches the device, so invalid calls return their status code (and a message) on any host.
+Pointers are placeholders: no call below gets past its failing check."""
+import ctypes
+
+import pytest
+import torch
+
+import tnpy_gb300._lib as L
+
+P = 16  # non-null placeholder address, never dereferenced by a call that fails validation
+
+
+def _err():
+    return L.lib.tnx_last_error().decode()
+
+
+def test_qr_rejects_wide_and_empty():
+    assert L.lib.tnx_qr(P, 4, 8, P, P, None, 0, None) == L.TNX_ERR_SHAPE
+    assert "m >= n" in _err()
+    assert L.lib.tnx_qr(P, 0, 0, P, P, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert L.lib.tnx_qr(None, 4, 4, P, P, None, 0, None) == L.TNX_ERR_INVALID_ARG
+
+
+def test_gauge_move_rejects_bad_arguments():
+    # precision, direction, sizes, and a split bond larger than the fused dimension
+    assert L.lib.tnx_gauge_move(1, P, P, 4, 2, 4, 4, 9, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert L.lib.tnx_gauge_move(2, P, P, 4, 2, 4, 4, 0, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert L.lib.tnx_gauge_move(1, P, P, 0, 2, 4, 4, 0, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert L.lib.tnx_gauge_move(1, P, P, 2, 2, 8, 4, 0, None, 0, None) == L.TNX_ERR_SHAPE
+    assert L.lib.tnx_gauge_move(-1, P, P, 8, 2, 2, 4, 0, None, 0, None) == L.TNX_ERR_SHAPE
+
+
+@pytest.mark.parametrize("max_iter,max_basis,tol,precision,expect", [
+    (0, 24, 1e-8, 0, L.TNX_ERR_INVALID_ARG),      # no matvec allowed
+    (100, 1, 1e-8, 0, L.TNX_ERR_INVALID_ARG),     # basis below 2
+    (100, 65, 1e-8, 0, L.TNX_ERR_INVALID_ARG),    # basis above the kernels' 64
+    (100, 24, -1.0, 0, L.TNX_ERR_INVALID_ARG),    # negative tolerance
+    (100, 24, 1e-8, 3, L.TNX_ERR_INVALID_ARG),    # unknown precision
+])
+def test_davidson_rejects_bad_arguments(max_iter, max_basis, tol, precision, expect):
+    ev, rn, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    st = L.lib.tnx_davidson1(P, P, P, P, 4, 2, 4, 5, 5, tol, max_iter, max_basis, precision, ctypes.byref(ev),
+                             ctypes.byref(rn), ctypes.byref(it), None, 0, None)
+    assert st == expect, _err()
+
+
+def test_davidson_rejects_large_mpo_bond():
+    ev, rn, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    st = L.lib.tnx_davidson1(P, P, P, P, 4, 2, 4, 33, 5, 1e-8, 100, 24, 0, ctypes.byref(ev), ctypes.byref(rn),
+                             ctypes.byref(it), None, 0, None)
+    assert st == L.TNX_ERR_SHAPE
+
+
+def test_gemm_oz_rejects_negative_size():
+    st = L.lib.tnx_gemm_oz(0, 0, -1, 4, 4, 1.0, P, 4, P, 4, 0.0, P, 4, None, 0, None)
+    assert st == L.TNX_ERR_INVALID_ARG
+    assert L.lib.tnx_gemm_oz(0, 0, 4, 4, 4, 1.0, None, 4, P, 4, 0.0, P, 4, None, 0, None) == L.TNX_ERR_INVALID_ARG
+
+
+def test_gauge_move_bad_direction_raises_keyerror():
+    """The Python mirror raises the reference's exception for a direction that is neither
+    left nor right (MatrixProductState.split_tensor, matrix_product_state.py:187-225)."""
+    import tnpy_gb300.kernels as K
+
+    a = torch.zeros((4, 2, 4), dtype=torch.float64)
+    nb = torch.zeros((4, 2, 4), dtype=torch.float64)
+    with pytest.raises(KeyError):
+        K.gauge_move(0, a, nb)
