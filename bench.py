@@ -355,8 +355,15 @@ def run_ours(a):
         energies.append(e)
         return e
 
+    # warm-up sweeps from the random MPS (the convergence the timed, converged sweeps follow):
+    # host wall time of each (device synchronised) and its energy
+    warmup_s = []
     for _ in range(a.warmup):
+        torch.cuda.synchronize()
+        tw = time.perf_counter()
         one_sweep()
+        torch.cuda.synchronize()
+        warmup_s.append(time.perf_counter() - tw)
 
     def barrier():
         if world > 1:
@@ -468,7 +475,8 @@ def run_ours(a):
             "e2e": {"value": world / e2e_t, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d + 8},
             "energy_last": energies[-1], "wall_s_per_step": wall / a.steps,
-            "davidson_matvecs_per_site_timed": mv_timed, "launches_before_timed": int(launches0)}
+            "davidson_matvecs_per_site_timed": mv_timed, "launches_before_timed": int(launches0),
+            "warmup_sweeps": {"s": warmup_s, "energy": energies[:a.warmup]}}
     # CPU restatement: per-site work scaled by the FP64 form's Davidson matvecs on the same state
     # (the reference's primme call uses the same tol), else by the timed mixed count + the anchor
     mv_cpu = mv_timed + 1.0
