@@ -1,0 +1,72 @@
+"""FiniteDMRG's host-side sweep loop and convergence rule without a GPU
+(finite_dmrg.py:173-257): directions alternate from a rightward first sweep, the run stops
+once |dE| < tol or after max_sweep sweeps, the energies of every sweep are returned, and the
+reference's warnings are logged. Sweeps are scripted; nothing touches the device."""
+import logging
+
+import numpy as np
+import pytest
+import torch
+
+from tnpy_gb300.finite_dmrg import Direction, FiniteDMRG, Metric
+
+
+def _scripted(energies, monkeypatch):
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    f = FiniteDMRG.__new__(FiniteDMRG)  # no environments: the loop logic only
+    f._energies, f._variances, f.sweep_seconds = [np.nan], [np.nan], []
+    f.compute_variance = False
+    f.directions = []
+    it = iter(energies)
+
+    def sweep(direction, tol=1e-8, **kwargs):
+        f.directions.append(direction)
+        return next(it)
+
+    f.sweep = sweep
+    return f
+
+
+def test_run_stops_at_tolerance(monkeypatch):
+    f = _scripted([-1.0, -1.5, -1.5 - 1e-12, -9.0], monkeypatch)
+    assert f.run(tol=1e-8, max_sweep=10) == [-1.0, -1.5, -1.5 - 1e-12]
+    assert f.directions == [Direction.RIGHTWARD, Direction.LEFTWARD, Direction.RIGHTWARD]
+    assert len(f.sweep_seconds) == 3
+
+
+def test_update_is_run(monkeypatch):
+    f = _scripted([-1.0, -1.0], monkeypatch)
+    assert f.update(tol=1e-8, max_sweep=5) == [-1.0, -1.0]
+
+
+def test_run_stops_at_max_sweep_with_warning(monkeypatch, caplog):
+    f = _scripted([-1.0, -2.0, -3.0, -4.0], monkeypatch)
+    with caplog.at_level(logging.WARNING, logger="tnpy"):
+        assert f.run(tol=1e-8, max_sweep=3) == [-1.0, -2.0, -3.0]
+    assert any("Maximum number of sweeps 3 is reached" in r.getMessage() for r in caplog.records)
+
+
+def test_large_decrease_logs_the_local_minimum_warning(monkeypatch, caplog):
+    f = _scripted([-1.0, -2.0, -2.0], monkeypatch)
+    with caplog.at_level(logging.WARNING, logger="tnpy"):
+        f.run(tol=1e-8, max_sweep=5)
+    assert any("Might be trapped in local minimum" in r.getMessage() for r in caplog.records)
+
+
+def test_converged_rule_matches_reference_cases():
+    f = FiniteDMRG.__new__(FiniteDMRG)
+    f._energies = [np.nan, -1.0]
+    assert not f._converged(1, 1e-8, 10, Metric.ENERGY)  # first sweep: gradient is NaN
+    f._energies = [np.nan, -1.0, -1.0 + 5e-9]
+    assert f._converged(2, 1e-8, 10, Metric.ENERGY)
+    f._energies = [np.nan, -1.0, -1.0 + 5e-6]  # energy went up by more than tol: keep sweeping
+    assert not f._converged(2, 1e-8, 10, Metric.ENERGY)
+    f._variances = [np.nan, 1e-3, 1e-3 - 1e-12]
+    assert f._converged(2, 1e-8, 10, Metric.VARIANCE)
+
+
+def test_measurements_need_a_run():
+    f = FiniteDMRG.__new__(FiniteDMRG)
+    f._energies = [np.nan]
+    with pytest.raises(RuntimeError):
+        _ = f.measurements
