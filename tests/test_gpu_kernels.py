@@ -333,6 +333,39 @@ def test_gauge_move_df64_rank_deficient(cuda, direction):
     assert np.max(np.abs(back - two)) <= 1e-11 * np.max(np.abs(two))
 
 
+def test_gemm_oz_nonfinite_propagates(cuda):
+    """A row of op(A) or a column of op(B) holding Inf / NaN gives NaN outputs (its integer slices
+    are not the value); every other output is the ordinary FP64-class product."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(17)
+    a, b = rng.standard_normal((300, 200)), rng.standard_normal((200, 150))
+    a[3, 5], a[7, 0], b[9, 11] = np.nan, np.inf, -np.inf
+    got = K.gemm_oz(_t(a, cuda), _t(b, cuda)).cpu().numpy()
+    bad_rows, bad_cols = [3, 7], [11]
+    assert np.isnan(got[bad_rows]).all() and np.isnan(got[:, bad_cols]).all()
+    keep_r = np.setdiff1d(np.arange(300), bad_rows)
+    keep_c = np.setdiff1d(np.arange(150), bad_cols)
+    ok = np.ix_(keep_r, keep_c)
+    ref = a[keep_r] @ b[:, keep_c]
+    bound = np.abs(a[keep_r]) @ np.abs(b[:, keep_c])
+    assert np.max(np.abs(got[ok] - ref) / bound) < 1e-13
+
+
+def test_gauge_move_mixed_propagates_nan(cuda):
+    """A NaN in the site tensor reaches Q and the neighbour in the FP64-class form, as it does in
+    FP64 arithmetic (numpy's QR), instead of being flushed to a finite value."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(23)
+    a = rng.standard_normal((64, 2, 128))
+    a[10, 1, 5] = np.nan
+    nb = rng.standard_normal((128, 2, 40))
+    ta, tn = _t(a, cuda), _t(nb, cuda)
+    K.gauge_move(1, ta, tn, precision="mixed")
+    assert np.isnan(ta.cpu().numpy()).any() and np.isnan(tn.cpu().numpy()).any()
+
+
 @pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
 @pytest.mark.parametrize("m,n,k", [(128, 64, 128), (300, 200, 500), (1000, 130, 1024), (5, 7, 3), (257, 65, 1500)])
 def test_gemm_oz(cuda, ta, tb, m, n, k):

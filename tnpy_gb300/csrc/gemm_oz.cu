@@ -49,7 +49,8 @@ constexpr uint32_t OZ_TMEM_COLS = 512;
 // Logical operand X(r, k) = src[r * rs + k * ks], rows x K (FP64). bmax[r] (zeroed before) =
 // largest biased FP64 exponent in row r, by atomicMax over CTAs of 32 rows x OZ_SCAN_K values of
 // k (the scan runs over the whole grid, not one CTA per row block). The row's scale exponent is
-// E = bmax - 1021 (|X(r, k)| < 2^(E-1)), 0 for an all-zero row: row_scale_exp.
+// E = bmax - 1021 (|X(r, k)| < 2^(E-1)), 0 for an all-zero row: row_scale_exp. bmax = 2047 marks
+// a row with Inf or NaN, whose outputs the GEMM epilogue sets to NaN.
 constexpr int OZ_SCAN_K = 256;
 __global__ void oz_rowmax_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
                                  int* __restrict__ bmax) {
@@ -270,11 +271,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
     if (ok && row < M) {
       const int er = row_scale_exp(ea[row]);
+      const bool row_nonfinite = ea[row] == 2047;  // the row holds Inf / NaN: its slices are not the value
       double* o = C + int64_t(row) * ldc + n0;
 #pragma unroll
       for (int j = 0; j < OZ_BN; ++j) {
         if (n0 + j < N) {
           double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
+          if (row_nonfinite || eb[n0 + j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
           v *= alpha;
           if (beta != 0.0) v = fma(beta, o[j], v);
           o[j] = v;

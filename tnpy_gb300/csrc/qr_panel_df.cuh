@@ -114,11 +114,17 @@ __device__ __forceinline__ df2 shfl_xor(df2 x, int o) {
   return {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
 }
 
-// double (exponent lowered by e: x 2^-e, exact) -> (hi, lo)
+// double (exponent lowered by e: x 2^-e, exact) -> (hi, lo); Inf and NaN stay non-finite
+// (split_df gives (+-inf, 0) / (NaN, 0)) so that they propagate through the factorisation
 __device__ __forceinline__ df2 split_scaled(double x, int e) {
   long long b = __double_as_longlong(x);
   const int ef = int((b >> 52) & 0x7ff);
-  if (ef == 0 || ef == 2047) {  // zero / subnormal (below 2^-1022: far below the split's range)
+  if (ef == 2047) {
+    df2 r;
+    split_df(x, r.h, r.l);
+    return r;
+  }
+  if (ef == 0) {  // zero / subnormal (below 2^-1022: far below the split's range)
     b &= (1LL << 63);
   } else if (ef - e <= 0) {
     b &= (1LL << 63);
