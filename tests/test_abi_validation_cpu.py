@@ -67,3 +67,17 @@ def test_gauge_move_bad_direction_raises_keyerror():
     nb = torch.zeros((4, 2, 4), dtype=torch.float64)
     with pytest.raises(KeyError):
         K.gauge_move(0, a, nb)
+
+
+@pytest.mark.parametrize("chi_l,d,chi_r,dl,dr", [
+    (2**40, 2, 2**40, 5, 5),          # the product of the bonds alone would wrap int64
+    (2**62, 2, 3, 5, 5),              # one huge bond
+    (2**21 + 1, 2, 1, 5, 5),          # one bond just above the static scratch
+    (8, 2**40, 8, 1, 1),              # a physical dimension that would wrap the product
+])
+def test_noalloc_matvec_rejects_sizes_that_would_overflow(chi_l, d, chi_r, dl, dr):
+    f = L.lib.tnx_matvec1_noalloc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int64] * 5 + [ctypes.c_void_p]
+    st = f(P, P, P, P, P, chi_l, d, chi_r, dl, dr, None)
+    assert st == L.TNX_ERR_SHAPE, _err()

@@ -70,3 +70,60 @@ def test_measurements_need_a_run():
     f._energies = [np.nan]
     with pytest.raises(RuntimeError):
         _ = f.measurements
+
+
+class _FakeSolverSite:
+    """Stands in for the device pieces of one_site_solver: a site tensor, an environment whose
+    site_operator returns placeholders, and a scripted davidson1."""
+
+    def __init__(self, results, monkeypatch):
+        import tnpy_gb300.kernels as K
+
+        self.calls = []
+        it = iter(results)
+
+        def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64", raise_on_fail=False):
+            self.calls.append(precision)
+            return next(it)
+
+        monkeypatch.setattr(K, "davidson1", davidson1)
+        f = FiniteDMRG.__new__(FiniteDMRG)
+        f._exact_solver_dim = 200
+        f.max_iter, f.max_basis = 400, 24
+        f.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0, "fp64_retries": 0}
+
+        class _Env:
+            mps = type("M", (), {"tensors": [torch.zeros((16, 2, 16), dtype=torch.float64)]})()
+
+            def site_operator(self, site):
+                return None, None, None
+
+        f._env = _Env()
+        self.f = f
+
+
+def test_unconverged_mixed_solve_is_continued_in_fp64(monkeypatch, caplog):
+    s = _FakeSolverSite([(-1.0, 0.5, 16, False), (-1.2, 1e-9, 30, True)], monkeypatch)
+    s.f.precision = "mixed"
+    with caplog.at_level(logging.INFO, logger="tnpy"):
+        e, _ = s.f.one_site_solver(0, 1e-8)
+    assert e == -1.2 and s.calls == ["mixed", "fp64"]
+    assert s.f.stats["fp64_retries"] == 1 and s.f.stats["unconverged"] == 0 and s.f.stats["matvecs"] == 46
+    assert not any(r.levelno >= logging.WARNING for r in caplog.records)
+
+
+def test_unconverged_solve_warns_every_time(monkeypatch, caplog):
+    s = _FakeSolverSite([(-1.0, 0.5, 400, False)] * 2, monkeypatch)
+    s.f.precision = "fp64"
+    with caplog.at_level(logging.WARNING, logger="tnpy"):
+        s.f.one_site_solver(0, 1e-8)
+        s.f.one_site_solver(0, 1e-8)
+    warned = [r for r in caplog.records if "did not converge" in r.getMessage()]
+    assert len(warned) == 2 and s.f.stats["unconverged"] == 2
+
+
+def test_unconverged_solve_can_raise(monkeypatch):
+    s = _FakeSolverSite([(-1.0, 0.5, 400, False)], monkeypatch)
+    s.f.precision = "fp64"
+    with pytest.raises(RuntimeError):
+        s.f.one_site_solver(0, 1e-8, raise_on_fail=True)

@@ -100,3 +100,43 @@ def test_davidson_mixed_from_random_start(cuda, chi):
     ef, rf, itf, okf = K.davidson1(L, W, R, x0.clone(), tol=1e-10, precision="fp64", max_iter=400)
     assert okm and okf, (em, rm, itm, ef, rf, itf)
     assert abs(em - ef) <= 1e-9 * abs(ef), (em, ef)
+
+
+@pytest.fixture(scope="module", params=[512, 1024])
+def swept_chain(request, cuda):
+    """XXZ(24, -0.5) at chi = 512 / 1024 (the middle bonds reach chi) after one rightward
+    mixed-precision sweep from the seeded random MPS: the local operators of a real sweep."""
+    import tnpy_gb300 as tg
+
+    chi = request.param
+    f = tg.FiniteDMRG(tg.model.XXZ(24, -0.5).mpo, bond_dim=chi, seed=11, compute_variance=False,
+                      precision="mixed")
+    f.sweep(tg.Direction.RIGHTWARD, tol=1e-8)
+    yield chi, f
+    del f
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("start", ["site_tensor", "random"])
+def test_davidson_mixed_hard_start_large_chi(cuda, swept_chain, start):
+    """chi = 512 and 1024 local problems from a far-off start: the middle site's tensor after the
+    sweep has moved past it (a left-orthonormal gauge tensor, as in a bench chain's middle site)
+    and a random vector. The mixed solver must converge, to the FP64 solver's eigenvalue within
+    |dE|/|E| <= 1e-9, and report convergence."""
+    from tnpy_gb300 import kernels as K
+
+    chi, f = swept_chain
+    site = 12
+    L, W, R = f.env.site_operator(site)
+    assert L.shape[0] == chi and R.shape[0] == chi
+    if start == "random":
+        g = torch.Generator(device="cpu").manual_seed(chi + 5)
+        x0 = torch.randn(f.mps.tensors[site].shape, generator=g, dtype=torch.float64).to(cuda)
+    else:
+        x0 = f.mps.tensors[site].clone()
+    em, rm, itm, okm = K.davidson1(L, W, R, x0.clone(), tol=1e-10, precision="mixed", max_iter=400)
+    stm = K.davidson1_stats()
+    ef, rf, itf, okf = K.davidson1(L, W, R, x0.clone(), tol=1e-10, precision="fp64", max_iter=400)
+    assert okf, (ef, rf, itf)
+    assert okm, (em, rm, itm, stm)
+    assert abs(em - ef) <= 1e-9 * abs(ef), (em, ef, stm)

@@ -18,8 +18,10 @@
 // anchored phase after one matvec (see davidson1).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <type_traits>
+#include <vector>
 
 #include "tnx_internal.cuh"
 
@@ -215,6 +217,25 @@ __global__ void restart_kernel(double* Hm, const double* evals, double* evecs) {
   evecs[0] = 1.0;
 }
 
+// out_v = V s, out_av = AV s over the first k basis vectors (the second vector of a GD+1 restart)
+template <typename T>
+__global__ void __launch_bounds__(DT) lincomb_kernel(const T* __restrict__ V, const T* __restrict__ AV, int64_t ldv,
+                                                    int k, const double* __restrict__ s, T* __restrict__ out_v,
+                                                    T* __restrict__ out_av, int64_t n) {
+  __shared__ T ss[MAXB];
+  if (threadIdx.x < k) ss[threadIdx.x] = T(s[threadIdx.x]);
+  __syncthreads();
+  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(gridDim.x) * DT) {
+    T xv = T(0), av = T(0);
+    for (int j = 0; j < k; ++j) {
+      xv = fma(ss[j], V[int64_t(j) * ldv + i], xv);
+      av = fma(ss[j], AV[int64_t(j) * ldv + i], av);
+    }
+    out_v[i] = xv;
+    out_av[i] = av;
+  }
+}
+
 inline int nchunk_for(int64_t n) {
   int64_t c = (n + DT * 4 - 1) / (DT * 4);
   if (c > 2 * 152) c = 2 * 152;
@@ -223,6 +244,7 @@ inline int nchunk_for(int64_t n) {
 
 struct DavWs {
   double *V, *AV, *x, *ax, *t, *diag, *Hm, *Hwork, *evals, *evecs, *jwork, *part, *scal;
+  double *xp, *axp;  // second vector of a GD+1 restart (previous Ritz vector, orthogonalised)
   void* mv;
   size_t mv_bytes;
   double *T1, *T2;  // FP64-class matvec scratch (also used by the anchored phase)
@@ -252,7 +274,8 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
          oHw = take(size_t(mb) * mb * 8), oev = take(size_t(mb) * 8), oevec = take(size_t(mb) * mb * 8),
          ojw = take(2 * size_t(mb) * mb * 8), opart = take(size_t(mb + 1) * nch * 8),
          oscal = take(size_t(4 * MAXB) * 8), oT1 = take(ne * 8), oT2 = take(ne * 8), omv = take(mv_bytes),
-         ooz = take(oz_bytes), od32 = take(precision == TNX_BF16X3 ? size_t(n) * 4 : 0);
+         ooz = take(oz_bytes), od32 = take(precision == TNX_BF16X3 ? size_t(n) * 4 : 0), oxp = take(n * 8),
+         oaxp = take(n * 8);
   if (w && base && off <= size) {
     char* b = static_cast<char*>(base);
     w->V = reinterpret_cast<double*>(b + oV);
@@ -275,6 +298,8 @@ size_t dav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t d
     w->oz = oz_bytes ? static_cast<void*>(b + ooz) : nullptr;
     w->oz_bytes = oz_bytes;
     w->diag32 = precision == TNX_BF16X3 ? reinterpret_cast<float*>(b + od32) : nullptr;
+    w->xp = reinterpret_cast<double*>(b + oxp);
+    w->axp = reinterpret_cast<double*>(b + oaxp);
   }
   return off;
 }
@@ -363,6 +388,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
 
   int k = 0, iters = 0, precond = 1;
   double theta = 0.0, rnorm = INFINITY, c0 = 1.0;
+  // Ritz coefficients of the last two Rayleigh-Ritz steps (host copies) for the GD+1 restart:
+  // s_prev is valid when it was computed on the basis V[0..k-1) that the current one extends.
+  std::vector<double> s_cur(MAXB, 0.0), s_prev(MAXB, 0.0), hm_host(size_t(MAXB) * MAXB, 0.0);
+  int cur_k = 0, prev_k = 0;
 
   // Rayleigh-Ritz on V[0..k), Ritz vector x, AV-combination ax, residual norm and the next
   // direction t; reads theta, ||r|| and the Ritz coefficient of V[0] back to the host.
@@ -376,6 +405,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     TNX_CUDA(cudaMemcpyAsync(host, w.evals, 8, cudaMemcpyDeviceToHost, st));
     TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
     TNX_CUDA(cudaMemcpyAsync(host + 2, w.evecs, 8, cudaMemcpyDeviceToHost, st));
+    std::swap(s_prev, s_cur);
+    prev_k = cur_k;
+    TNX_CUDA(cudaMemcpyAsync(s_cur.data(), w.evecs, size_t(k) * 8, cudaMemcpyDeviceToHost, st));
+    cur_k = k;
     if (dflag) TNX_CUDA(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
     TNX_CUDA(cudaStreamSynchronize(st));
     if (hflag) {
@@ -442,18 +475,82 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     restart_kernel<<<1, 1, 0, st>>>(w.Hm, w.evals, w.evecs);
     TNX_LAUNCH_CHECK();
     k = 1;
+    cur_k = prev_k = 0;
     return TNX_OK;
   };
+
+  // GD+1 restart (the "+k" of primme's GD+k, k = 1): keep the Ritz vector x = V s and the
+  // previous step's Ritz vector V s_prev orthogonalised against it, s' = s_prev - (s.s_prev) s
+  // (V is orthonormal, so this is done on the coefficients). The 2 x 2 projected matrix is
+  // [s s']^T H_k [s s'] from the current projected matrix H_k. Far from convergence this keeps
+  // the search direction a one-vector restart throws away; it falls back to that restart when
+  // the previous vector is not available or lies along x.
+  auto restart_plus = [&](const auto& vs) -> int {
+    using T = std::remove_pointer_t<decltype(vs.V)>;
+    if (prev_k != k - 1 || cur_k != k || k < 2) return restart(vs);
+    double dot = 0.0;
+    for (int j = 0; j < k - 1; ++j) dot += s_cur[j] * s_prev[j];
+    double sp[MAXB], nrm = 0.0;
+    for (int j = 0; j < k; ++j) {
+      sp[j] = (j < k - 1 ? s_prev[j] : 0.0) - dot * s_cur[j];
+      nrm += sp[j] * sp[j];
+    }
+    nrm = sqrt(nrm);
+    if (!(nrm > 1e-6)) return restart(vs);
+    for (int j = 0; j < k; ++j) sp[j] /= nrm;
+    TNX_CUDA(cudaMemcpy2DAsync(hm_host.data(), size_t(k) * 8, w.Hm, size_t(mb) * 8, size_t(k) * 8, size_t(k),
+                               cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaStreamSynchronize(st));
+    double h01 = 0.0, h11 = 0.0;
+    for (int i = 0; i < k; ++i) {
+      double hs = 0.0;
+      for (int j = 0; j < k; ++j) hs += hm_host[size_t(i) * k + j] * sp[j];
+      h01 += s_cur[i] * hs;
+      h11 += sp[i] * hs;
+    }
+    double* dsp = w.scal + 2 * MAXB;  // free part of the scalar block
+    TNX_CUDA(cudaMemcpyAsync(dsp, sp, size_t(k) * 8, cudaMemcpyHostToDevice, st));
+    T* xp = reinterpret_cast<T*>(w.xp);
+    T* axp = reinterpret_cast<T*>(w.axp);
+    lincomb_kernel<T><<<sblocks, DT, 0, st>>>(vs.V, vs.AV, n, k, dsp, xp, axp, n);
+    TNX_LAUNCH_CHECK();
+    TNX_CUDA(cudaMemcpyAsync(vs.V, vs.x, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    TNX_CUDA(cudaMemcpyAsync(vs.AV, vs.ax, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    TNX_CUDA(cudaMemcpyAsync(vs.V + n, xp, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    TNX_CUDA(cudaMemcpyAsync(vs.AV + n, axp, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    const double h2[4] = {theta, h01, h01, h11};
+    TNX_CUDA(cudaMemcpy2DAsync(w.Hm, size_t(mb) * 8, h2, 16, 16, 2, cudaMemcpyHostToDevice, st));
+    TNX_CUDA(cudaStreamSynchronize(st));  // h2 / sp are host stack memory
+    k = 2;
+    cur_k = prev_k = 0;
+    return TNX_OK;
+  };
+
+  // max |diag H|: with 2 |theta| it estimates |H| for the floors and bounds below (the diagonal
+  // alone is a lower bound of the spectral radius and catches operators whose lowest eigenvalue
+  // is small against their width)
+  absmax_kernel<<<nch, DT, 0, st>>>(w.diag, n, w.part, nch);
+  TNX_LAUNCH_CHECK();
+  max_reduce_kernel<<<1, 32, 0, st>>>(w.part, nch, w.scal + MAXB + 3);
+  TNX_LAUNCH_CHECK();
+  double hdiag = 0.0;
+  TNX_CUDA(cudaMemcpyAsync(&hdiag, w.scal + MAXB + 3, 8, cudaMemcpyDeviceToHost, st));
+  TNX_CUDA(cudaStreamSynchronize(st));
+  auto hscale = [&]() { return fmax(fmax(2.0 * fabs(theta), hdiag), 1.0); };
 
   bool converged = false;
   int restarts = 0, anchors = 0, phase1 = 0;
   // Stagnation: the split-BF16 operand is not exactly symmetric, so the residual of the
-  // mixed operator stops falling at ~1e-5 |H| (its rounding floor); the first phase ends when
-  // the residual has not improved by 10% within `patience` matvecs. The FP64 form uses a longer
-  // patience as a safeguard.
+  // mixed operator stops falling at ~1e-5 |H| (its rounding floor). The first phase treats
+  // "no 10% gain within `patience` matvecs" as that floor only when the residual is already
+  // within ~100x of it (below 1e-3 |H|); further out a Davidson residual can plateau while
+  // theta still falls (hard starts, small local gaps), and the phase keeps expanding, with
+  // GD+1 restarts, until max_iter. The FP64 forms treat stagnation as their floor below
+  // 1e-11 |H| (tol = 0 asks for machine accuracy, as primme's default does).
   double best = INFINITY;
   int best_it = 0;
   const int patience = mixed ? 8 : 40;
+  const double mixed_floor_band = 1e-3, fp64_floor_band = 1e-11;
   // The mixed form hands over to the anchored phase once the split-BF16 residual is below
   // 3e-6 |theta| or has stagnated at its ~1e-5 |H| floor (an earlier hand-over can leave the
   // solve on an excited state), and then converges the FP64-class residual to
@@ -498,13 +595,17 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       best = rnorm;
       best_it = iters;
     } else if (iters - best_it >= patience) {
-      converged = mixed;  // at the mixed rounding floor: done; FP64: report non-convergence
-      break;
+      if (rnorm <= (mixed ? mixed_floor_band : fp64_floor_band) * hscale()) {
+        converged = true;  // at the rounding floor (mixed: the anchored phase takes over)
+        break;
+      }
+      best = rnorm;  // far above the floor: a plateau, not the floor; keep expanding
+      best_it = iters;
     }
     if (iters >= max_iter) break;
     precond = 1;
     if (k == mb) {
-      TNX_TRY(f32 ? restart(v32) : restart(v64));
+      TNX_TRY(f32 ? restart_plus(v32) : restart_plus(v64));
       ++restarts;
     }
   }
@@ -518,17 +619,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     // vector outside x. The residual of the anchored Ritz pair is therefore FP64-class
     // while 3e-5 |H| |c| stays below half the target; otherwise (or on stagnation) the phase
     // re-anchors at the current Ritz vector with another FP64-class matvec.
-    const int max_anchor = 6;
+    // anchors are FP64-class products (several split-BF16 matvecs each); they are bounded by
+    // max_iter / 8 (at least 6), the split-BF16 products by max_iter
+    const int max_anchor = std::max(6, max_iter / 8);
     const double eps_h = 3e-5;  // bound on the split-BF16 matvec error relative to |H|
-    // |H| for the bound: max(2 |theta|, max |diag H|); the diagonal alone is a lower bound of the
-    // spectral radius and catches operators whose lowest eigenvalue is small against their width
-    absmax_kernel<<<nch, DT, 0, st>>>(w.diag, n, w.part, nch);
-    TNX_LAUNCH_CHECK();
-    max_reduce_kernel<<<1, 32, 0, st>>>(w.part, nch, w.scal + MAXB + 3);
-    TNX_LAUNCH_CHECK();
-    double hdiag = 0.0;
-    TNX_CUDA(cudaMemcpyAsync(&hdiag, w.scal + MAXB + 3, 8, cudaMemcpyDeviceToHost, st));
-    TNX_CUDA(cudaStreamSynchronize(st));
     converged = false;
     for (int anchor = 0;; ++anchor) {
       if (anchor == 0 && f32) {
@@ -552,8 +646,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       double drift = 0.0;  // sum of |c| over restarts inside this anchor
       auto bound_ok = [&]() {
         const double c = sqrt(fmax(1.0 - c0 * c0, 0.0));
-        const double hs = fmax(fmax(2.0 * fabs(theta), hdiag), 1.0);
-        return eps_h * hs * (drift + c) <= 0.5 * mixed_rtol * fmax(1.0, fabs(theta));
+        return eps_h * hscale() * (drift + c) <= 0.5 * mixed_rtol * fmax(1.0, fabs(theta));
       };
       if (rnorm <= mixed_rtol * fmax(1.0, fabs(theta))) {
         converged = true;
@@ -563,9 +656,9 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
       best = rnorm;
       best_it = iters;
       // The bound decides whether a converged residual is accepted and, within 100x of the
-      // target, when to refresh the anchor; while the residual is still large the phase keeps
-      // expanding (a Davidson whose row 0 is exact) and re-anchors on stagnation or once the
-      // Ritz vector has moved far from the anchor.
+      // target, when to refresh the anchor (also once the Ritz vector has moved far from the
+      // anchor there); while the residual is still large the phase keeps expanding (a Davidson
+      // whose row 0 is exact) and re-anchors only on stagnation.
       for (;;) {
         bool fell_in = false;
         TNX_TRY(expand(v64, true, &fell_in));
@@ -574,9 +667,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
           if (bound_ok()) converged = true;
           break;
         }
+        const bool near = rnorm < 100.0 * mixed_rtol * fmax(1.0, fabs(theta));
         // close to the target but the anchor no longer vouches for the residual: refresh it
-        if (!bound_ok() && rnorm < 100.0 * mixed_rtol * fmax(1.0, fabs(theta))) break;
-        if (drift + sqrt(fmax(1.0 - c0 * c0, 0.0)) > 0.3) break;
+        if (near && !bound_ok()) break;
+        if (near && drift + sqrt(fmax(1.0 - c0 * c0, 0.0)) > 0.3) break;
         if (rnorm < 0.9 * best) {
           best = rnorm;
           best_it = iters;

@@ -58,8 +58,13 @@ extern "C" int tnx_matvec1_noalloc(const double* L, const double* W, const doubl
                                    int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, void* stream) {
   TNX_CHECK_ARG(L && W && R && x && y, "null pointer");
   TNX_CHECK_ARG(chi_l > 0 && d > 0 && chi_r > 0 && dl > 0 && dr > 0, "non-positive dimension");
-  TNX_CHECK_SHAPE(dl * d <= 64 && dr * d <= 64, "MPO bond too large: dl*d=%lld dr*d=%lld (max 64)",
-                  (long long)(dl * d), (long long)(dr * d));
+  TNX_CHECK_SHAPE(d <= 64 && dl <= 64 && dr <= 64 && dl * d <= 64 && dr * d <= 64,
+                  "MPO bond too large: dl*d=%lld dr*d=%lld (max 64)", (long long)(dl * d), (long long)(dr * d));
+  // each bond alone must fit before the product is formed: with chi_l, chi_r <= 2^21 and
+  // d, dl, dr <= 64 the product below stays under 2^60 and cannot wrap
+  TNX_CHECK_SHAPE(chi_l <= kNoallocElems && chi_r <= kNoallocElems,
+                  "tnx_matvec1_noalloc: bond %lld x %lld exceeds the static scratch of %lld elements",
+                  (long long)chi_l, (long long)chi_r, (long long)kNoallocElems);
   const int64_t need = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);
   TNX_CHECK_SHAPE(need <= kNoallocElems,
                   "tnx_matvec1_noalloc: chi_l*d*chi_r*max(dl,dr) = %lld exceeds the static scratch of %lld "

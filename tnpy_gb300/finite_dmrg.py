@@ -82,7 +82,8 @@ class FiniteDMRG:
         self._energies = [np.nan]
         self._variances = [np.nan]
         self.sweep_seconds: list[float] = []
-        self.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0}
+        self.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0,
+                      "fp64_retries": 0}
 
     # ---- properties (finite_dmrg.py:78-95) ----------------------------------------------
     @property
@@ -117,7 +118,14 @@ class FiniteDMRG:
     # ---- local steps --------------------------------------------------------------------
     def one_site_solver(self, site: int, tol: float = 1e-8, **kwargs):
         """Lowest eigenpair at ``site`` (finite_dmrg.py:97-111). Returns (energy, psi) with
-        psi a device tensor of the site's shape."""
+        psi a device tensor of the site's shape.
+
+        An iterative solve that ends without meeting ``tol`` is never passed on silently (the
+        reference's primme.eigsh raises on non-convergence by default): a mixed-precision
+        solve is first continued by the FP64 Davidson from the vector it reached
+        (``stats['fp64_retries']``); a solve that still fails is logged as a warning on the
+        ``tnpy`` logger and counted in ``stats['unconverged']``, or raises RuntimeError with
+        ``raise_on_fail=True``."""
         x = self.mps.tensors[site]
         if x.numel() < self._exact_solver_dim:
             self.stats["dense_solves"] += 1
@@ -127,13 +135,25 @@ class FiniteDMRG:
         self.stats["iterative_solves"] += 1
         psi = x.clone()
         L, W, R = self._env.site_operator(site)
-        e, rn, its, ok = K.davidson1(L, W, R, psi, tol=tol, max_iter=kwargs.get("max_iter", self.max_iter),
-                                     max_basis=kwargs.get("max_basis", self.max_basis),
-                                     precision=kwargs.get("precision", self.precision))
+        max_iter = kwargs.get("max_iter", self.max_iter)
+        max_basis = kwargs.get("max_basis", self.max_basis)
+        precision = kwargs.get("precision", self.precision)
+        e, rn, its, ok = K.davidson1(L, W, R, psi, tol=tol, max_iter=max_iter, max_basis=max_basis,
+                                     precision=precision)
         self.stats["matvecs"] += its
+        if not ok and K.precision_code(precision) != K.precision_code("fp64"):
+            self.stats["fp64_retries"] += 1
+            logger.info(f"site {site}: {precision} Davidson stopped at residual {rn:.3e} after {its} matvecs; "
+                        f"continuing in FP64")
+            e, rn, its, ok = K.davidson1(L, W, R, psi, tol=tol, max_iter=max_iter, max_basis=max_basis,
+                                         precision="fp64")
+            self.stats["matvecs"] += its
         if not ok:
             self.stats["unconverged"] += 1
-            logger.debug(f"site {site}: Davidson stopped at residual {rn:.3e} after {its} matvecs")
+            msg = f"site {site}: Davidson did not converge (residual {rn:.3e} after {its} matvecs, tol {tol:.1e})"
+            if kwargs.get("raise_on_fail", False):
+                raise RuntimeError(msg)
+            logger.warning(msg)
         return e, psi
 
     def two_site_solver(self, site: int, tol: float = 1e-8, **kwargs):
