@@ -26,6 +26,8 @@ import tempfile
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -46,7 +48,7 @@ def parse():
     p.add_argument("--seed", type=int, default=1234)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the matvec-form and tSDRG measurements")
-    p.add_argument("--tsdrg-realizations", type=int, default=64)
+    p.add_argument("--tsdrg-realizations", type=int, default=1024)
     p.add_argument("--chains", type=int, default=64, help="independent chi=64 chains of the batched fDMRG line")
     return p.parse_args()
 
@@ -101,58 +103,144 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ------------------------------------------------------------------ CPU sample (oracle)
-# Davidson matvecs per site of the FP64 GPU form on the timed sweeps' converged state (bench
-# field fp64_sweep.fp64.matvecs_per_site, measured 1.78 at n=100, chi=1024): the work per site of
-# the reference's primme call (same tol) where this run does not measure it (reference arm)
-REF_MATVECS_PER_SITE = 1.8
+# ------------------------------------------------------------------ CPU restatement (oracle)
+def sweep_site_weight(n: int, chi: int, d: int = 2) -> float:
+    """Sum over the n-1 site updates of one sweep of chi_l chi_r max(chi_l, chi_r) / chi^3: the
+    number of full-chi site updates a sweep's work equals (the matvec, environment update and
+    gauge move of a site scale with that product; 81.1 for n=100, chi=1024, where 80 of the 99
+    sites have full bonds)."""
+    from oracle import mps as omps
+
+    dims = omps.bond_dims(n, chi, d)
+    return sum(dims[i] * dims[i + 1] * max(dims[i], dims[i + 1]) for i in range(n - 1)) / float(chi) ** 3
 
 
-def cpu_sample(a, matvecs_per_site: float | None = None):
-    """CPU restatement of the reference's per-site work at the bench's n and chi, timed on the
-    host cores: one-site matvec (the primme callback), SVD gauge move (split_tensor) and
-    environment update, each repeated for a bounded time at a middle site of the chain.
-    A site update costs matvecs_per_site matvecs (the eigensolver) + 1 split + 1 environment
-    update; a sweep is n-1 site updates. matvecs_per_site is the FP64 GPU form's average on the
-    same state when measured in the same run, else REF_MATVECS_PER_SITE."""
+class CpuBulkPair:
+    """Two neighbouring bulk sites i, i+1 of a chain in the CPU restatement, with the centre on
+    site i: L_i, R_{i+1} fixed, the two site tensors and their MPO tensors. ``step`` performs one
+    site update of FiniteDMRG.sweep (tnpy/finite_dmrg.py:143-171) in numpy: the lowest eigenpair
+    from the current site tensor (oracle.eigsh_gd, the GD+1 restatement of primme.eigsh, at the
+    sweep's tol), the 1e-5 perturbation, the SVD gauge move onto the neighbour and the
+    environment update; the updates alternate rightward at i and leftward at i+1, i.e. a sweep
+    bouncing between the two sites."""
+
+    def __init__(self, L, Wi, Wj, R, ai, aj, tol):
+        from oracle import mps as omps
+
+        self.L, self.Wi, self.Wj, self.R = L, Wi, Wj, R
+        self.ai, self.aj = ai, aj
+        self.tol = tol
+        self.Ri = omps.update_right(R, aj, Wj)  # R_i for the first (rightward) update at i
+        self.Lj = None
+        self.right = True
+        self.matvecs = 0
+        self.energy = None
+
+    def step(self, tol: float | None = None):
+        from oracle import eigsh_gd
+        from oracle import mps as omps
+
+        if self.right:
+            L, W, R, x = self.L, self.Wi, self.Ri, self.ai
+        else:
+            L, W, R, x = self.Lj, self.Wj, self.R, self.aj
+        shape = x.shape
+        e, v, mv, _ = eigsh_gd.eigsh_gd(lambda u: omps.one_site_matvec(L, W, R, u.reshape(shape)).reshape(-1),
+                                        x, tol=self.tol if tol is None else tol)
+        psi = v.reshape(shape)
+        psi = psi + 1e-5 * omps.one_site_matvec(L, W, R, psi)
+        pair = [self.ai, self.aj]
+        if self.right:
+            pair[0] = psi
+            omps.split_tensor(pair, 0, rightward=True)
+            self.ai, self.aj = pair
+            self.Lj = omps.update_left(self.L, self.ai, self.Wi)
+        else:
+            pair[1] = psi
+            omps.split_tensor(pair, 1, rightward=False)
+            self.ai, self.aj = pair
+            self.Ri = omps.update_right(self.R, self.aj, self.Wj)
+        self.right = not self.right
+        self.matvecs += mv + 1
+        self.energy = e
+        return e, mv
+
+
+def cpu_pair_from_random_mps(a):
+    """A bulk pair with full chi on both sides, built in numpy from a seeded random MPS: the middle
+    sites of XXZ(n_env, delta) with n_env = 2 ceil(log2 chi) + 2 (22 for chi = 1024), whose middle
+    bonds reach chi, so that the local problem has the shape of every bulk site of the bench
+    chain (L, R: chi x D x chi) while its environments take only ~n_env small contractions to
+    build. Right-canonical tensors, centre moved from site 0 to the pair by QR."""
+    import math
+
     import numpy as np
 
     from oracle import models as om
     from oracle import mps as omps
 
-    n, chi = a.n, a.chi
-    site = n // 2
-    w = om.uniform(om.xxz_mpo(n, a.delta))[site]
-    rng = np.random.RandomState(a.seed)
-    dims = omps.bond_dims(n, chi, 2)
-    cl, cr = dims[site], dims[site + 1]
-    L = rng.standard_normal((cl, 5, cl))
-    R = rng.standard_normal((cr, 5, cr))
-    x = rng.standard_normal((cl, 2, cr))
-    nb = rng.standard_normal((cr, 2, dims[site + 2]))
+    half = max(1, math.ceil(math.log2(a.chi)))
+    n = min(a.n, 2 * half + 2)
+    i = n // 2 - 1
+    W = om.uniform(om.xxz_mpo(n, a.delta))
+    mps = omps.random_mps(n, a.chi, 2, seed=a.seed)
+    for s in range(i):  # gauge the centre onto site i
+        cl, d, cr = mps[s].shape
+        q, r = np.linalg.qr(mps[s].reshape(cl * d, cr))
+        mps[s] = q.reshape(cl, d, q.shape[1])
+        mps[s + 1] = np.tensordot(r, mps[s + 1], axes=([1], [0]))
+    L = np.ones((1, 1, 1))
+    for s in range(i):
+        L = omps.update_left(L, mps[s], W[s])
+    R = np.ones((1, 1, 1))
+    for s in range(n - 1, i + 1, -1):
+        R = omps.update_right(R, mps[s], W[s])
+    return L, W[i], W[i + 1], R, mps[i], mps[i + 1]
 
-    def timed(fn, budget):
-        fn()
-        t0, k = time.perf_counter(), 0
-        while True:
-            fn()
-            k += 1
-            dt = time.perf_counter() - t0
-            if dt > budget or k >= 50:
-                return dt / k
 
-    t_mv = timed(lambda: omps.one_site_matvec(L, w, R, x), 4.0)
-    t_split = timed(lambda: omps.split_tensor([x.copy(), nb.copy()], 0, rightward=True), 4.0)
-    t_env = timed(lambda: omps.update_left(L, x, w), 4.0)
-    mv = REF_MATVECS_PER_SITE if matvecs_per_site is None else float(matvecs_per_site)
-    per_site = mv * t_mv + t_split + t_env
-    return {"value": 1.0 / (per_site * (n - 1)), "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"numpy/scipy FP64 restatement at site {site} of n={n}, chi={chi} (bonds {cl}x{cr}): "
-                      f"matvec {t_mv * 1e3:.1f} ms, SVD split {t_split * 1e3:.1f} ms, env update "
-                      f"{t_env * 1e3:.1f} ms, each repeated for ~4 s; site update = {mv:.2f} matvecs + "
-                      f"split + env, {n - 1} site updates per sweep (full-chi site cost for every site)",
-            "seconds_per_site": per_site, "matvecs_per_site": mv,
-            "matvec_tflops": (40 * cl * cr * max(cl, cr) + 200 * cl * cr) / t_mv / 1e12}
+def cpu_site_updates(pair: "CpuBulkPair", steps: int, warmup: int, prepare_s: float = 0.0):
+    """Per-step wall times of ``steps`` timed site updates after ``warmup`` untimed ones; with
+    prepare_s > 0 the pair is first swept (untimed) until its energy settles to the pair's tol
+    or prepare_s seconds pass, so that the timed updates see a converged state as the timed GPU
+    sweeps do."""
+    t_prep = time.perf_counter()
+    prep = 0
+    if prepare_s > 0:
+        # loose local tolerance first (the random start is far from the pair's ground state),
+        # then the sweep's tol until the energy settles
+        last = None
+        while time.perf_counter() - t_prep < prepare_s:
+            loose = prep < 2
+            e, _ = pair.step(tol=1e-5 if loose else None)
+            prep += 1
+            if not loose and last is not None and abs(e - last) < pair.tol * max(1.0, abs(e)):
+                break
+            last = e
+    prep_s = time.perf_counter() - t_prep
+    for _ in range(warmup):
+        pair.step()
+    mv0 = pair.matvecs
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        pair.step()
+        times.append(time.perf_counter() - t0)
+    return {"times": times, "matvecs_per_update": (pair.matvecs - mv0) / max(1, steps),
+            "prepare_updates": prep, "prepare_s": prep_s}
+
+
+def cpu_result(a, res, origin: str, kind: str = "port"):
+    mean = statistics.fmean(res["times"])
+    w = sweep_site_weight(a.n, a.chi)
+    return {"value": 1.0 / (mean * w), "unit": "sweeps/s", "cores": os.cpu_count(), "kind": kind,
+            "sample": f"{len(res['times'])} timed site updates (after the warm-up) of the numpy/scipy FP64 "
+                      f"restatement bouncing between bulk sites {a.n // 2} and {a.n // 2 + 1} of XXZ(n={a.n}) at "
+                      f"chi={a.chi}, {origin}; each: GD+1 eigensolver (primme restatement) at tol {a.tol:g} from the "
+                      f"current site tensor, 1e-5 perturbation, SVD gauge move, environment update; "
+                      f"sweep time = mean site update x {w:.1f} full-chi site equivalents of the {a.n - 1} sites",
+            "seconds_per_site_update": mean, "site_updates_timed": len(res["times"]),
+            "matvecs_per_site_update": res["matvecs_per_update"], "sweep_site_weight": w,
+            "prepare_updates": res["prepare_updates"], "prepare_s": res["prepare_s"]}
 
 
 # ------------------------------------------------------------------ secondary measurements
@@ -190,6 +278,7 @@ def matvec_forms(f, site: int):
         torch.cuda.synchronize()
         evs[form] = {"eval": e, "residual": rn, "matvecs": its, "converged": bool(ok),
                      "s": time.perf_counter() - t0}
+    evs["local_dE_rel_mixed_vs_fp64"] = abs(evs["mixed"]["eval"] - evs["fp64"]["eval"]) / abs(evs["fp64"]["eval"])
     out["local_eigensolve"] = evs
     out["local_dE_rel_mixed_vs_fp64"] = abs(evs["mixed"]["eval"] - evs["fp64"]["eval"]) / abs(evs["fp64"]["eval"])
     return out
@@ -199,12 +288,13 @@ def fp64_sweep(f, direction, tol: float, mixed_s: float):
     """The plain FP64 GPU form against the mixed form on the same state: both chains start from a
     copy of the bench chain's current MPS (environments rebuilt in each form) and sweep once in
     the same direction; reports the FP64 sweep's seconds, the speed-up of the mixed form's timed
-    sweeps over it, and |dE|/|E| between the two energies after the sweep."""
+    sweeps over it, |dE|/|E| between the two energies after the sweep and the largest difference
+    of the local <Sz_i> of the two states."""
     import torch
 
     import tnpy_gb300 as tg
 
-    out = {}
+    out, sz = {}, {}
     for form in ("fp64", "mixed"):
         mps = tg.MatrixProductState([t.clone() for t in f.mps.tensors], device=f.mps.device)
         g = tg.FiniteDMRG(f.env.mpo, bond_dim=f.bond_dim, mps=mps, precision=form, compute_variance=False,
@@ -214,18 +304,129 @@ def fp64_sweep(f, direction, tol: float, mixed_s: float):
         e = g.sweep(direction, tol=tol)
         torch.cuda.synchronize()
         out[form] = {"s": time.perf_counter() - t0, "energy": e,
-                     "matvecs_per_site": g.stats["matvecs"] / max(1, g.stats["iterative_solves"])}
+                     "matvecs_per_site": g.stats["matvecs"] / max(1, g.stats["iterative_solves"]),
+                     "unconverged": g.stats["unconverged"], "df64_retries": g.stats["df64_retries"]}
+        sz[form] = tg.MatrixProductStateMeasurements(g.mps).local_sz()
         del g, mps
         torch.cuda.empty_cache()
     out["speedup_mixed_timed_vs_fp64"] = out["fp64"]["s"] / mixed_s
     out["dE_rel_mixed_vs_fp64"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])
+    out["max_sz_err_mixed_vs_fp64"] = float(abs(sz["mixed"] - sz["fp64"]).max())
     return out
 
 
-def tsdrg_rate(n_real: int, with_cpu: bool):
+def config1_line(with_cpu: bool):
+    """Plain FP64 fDMRG of XXZ(32, delta=-0.5) (H = sum SxSx + SySy + 0.5 SzSz up to a sublattice
+    rotation), chi=32, seeded random MPS, tol 1e-8, at most 10 sweeps: seconds per sweep on the
+    GPU, the same run of the CPU restatement timed beside it, their final energies, and the ED
+    cross-check at n=12 (GPU fDMRG against the dense ground-state energy)."""
+    import torch
+
+    import tnpy_gb300 as tg
+
+    n, chi = 32, 32
+    f = tg.FiniteDMRG(tg.model.XXZ(n, -0.5).mpo, bond_dim=chi, seed=1234, precision="fp64", compute_variance=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    es = f.run(tol=1e-8, max_sweep=10)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out = {"workload": "fdmrg_xxz_n32_chi32_fp64", "sweeps": len(es), "seconds": dt,
+           "s_per_sweep": statistics.fmean(f.sweep_seconds), "energy": es[-1], "unconverged": f.stats["unconverged"]}
+    g = tg.FiniteDMRG(tg.model.XXZ(12, -0.5).mpo, bond_dim=chi, seed=1234, precision="fp64", compute_variance=False)
+    e12 = g.run(tol=1e-10, max_sweep=10)[-1]
+    out["n12_energy"] = e12
+    if with_cpu:
+        from oracle import dmrg as odmrg
+        from oracle import models as om
+        from oracle import operators as oops
+
+        e_ed = float(np.linalg.eigvalsh(oops.full_hamiltonian(om.xxz_mpo(12, -0.5)))[0])
+        out["ed_n12_energy"] = e_ed
+        out["dE_rel_n12_vs_ed"] = abs(e12 - e_ed) / abs(e_ed)
+        o = odmrg.FiniteDMRG(om.xxz_mpo(n, -0.5), chi=chi, seed=1234, eig_tol=1e-10)
+        t0 = time.perf_counter()
+        eo = o.run(tol=1e-8, max_sweep=10, with_variance=False)
+        tc = time.perf_counter() - t0
+        out["dE_rel_vs_cpu_restatement"] = abs(es[-1] - eo[-1]) / abs(eo[-1])
+        out["cpu_baseline"] = {"value": len(eo) / tc, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+                               "s_per_sweep": tc / len(eo), "sweeps": len(eo),
+                               "sample": "the whole run (same seed, tol, sweep limit) of the numpy restatement"}
+    out["value"] = len(es) / dt
+    out["unit"] = "sweeps/s"
+    return out
+
+
+def config2_ramp_line(precision: str = "mixed"):
+    """Config 2's chi ramp on XXZ(100, delta=-0.5): chi 256 -> 512 -> 1024 from the seeded random
+    MPS, two sweeps per stage and then sweeps to |dE| < 1e-8 at chi=1024 (FiniteDMRG.ramp): per
+    stage the sweeps, seconds, energy, middle-bond truncation error (weight beyond the previous
+    chi) and smallest kept Schmidt weight, and the time to solution of the whole ramp."""
+    import torch
+
+    import tnpy_gb300 as tg
+
+    f = tg.FiniteDMRG(tg.model.XXZ(100, -0.5).mpo, bond_dim=256, seed=1234, precision=precision,
+                      compute_variance=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    stages = f.ramp([256, 512, 1024], sweeps_per_stage=2, tol=1e-8, max_sweep=12)
+    dt = time.perf_counter() - t0
+    out = {"workload": f"fdmrg_xxz_n100_ramp256_512_1024_{precision}", "seconds_total": dt,
+           "unconverged": f.stats["unconverged"], "df64_retries": f.stats["df64_retries"], "stages": []}
+    for st in stages:
+        out["stages"].append({k: st[k] for k in ("chi", "sweeps", "seconds", "energy", "smallest_kept_weight")
+                              if k in st} | ({"truncation_error_prev_chi": st["truncation_error_prev_chi"]}
+                                             if "truncation_error_prev_chi" in st else {}))
+    del f
+    torch.cuda.empty_cache()
+    return out
+
+
+def config3_line(with_cpu: bool):
+    """Random-field Heisenberg RandomHeisenberg(200, h=3, seed=7), chi=512: the mixed form with
+    FP32 environment storage swept to convergence from the seeded random MPS, then the plain
+    FP64 form converged from a copy of that state; seconds per sweep of each, |dE|/|E|, the
+    largest difference of the middle-bond entanglement spectra and of the local <Sz_i>."""
+    import torch
+
+    import tnpy_gb300 as tg
+
+    n, chi = 200, 512
+    mpo = tg.model.RandomHeisenberg(n, h=3.0, seed=7).mpo
+    f = tg.FiniteDMRG(mpo, bond_dim=chi, seed=1234, precision="mixed", env_precision="fp32", compute_variance=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    em = f.run(tol=1e-9, max_sweep=10)
+    torch.cuda.synchronize()
+    tm = time.perf_counter() - t0
+    g = tg.FiniteDMRG(mpo, bond_dim=chi, mps=tg.MatrixProductState([t.clone() for t in f.mps.tensors]),
+                      precision="fp64", compute_variance=False)
+    ef = g.run(tol=1e-10, max_sweep=6)
+    bond = n // 2 - 1
+    lam_m, lam_f = f.measurements.entanglement_spectrum(bond), g.measurements.entanglement_spectrum(bond)
+    sz_m, sz_f = f.measurements.local_sz(), g.measurements.local_sz()
+    out = {"workload": "fdmrg_random_heisenberg_n200_h3_chi512", "mixed_env": "fp32",
+           "mixed": {"sweeps": len(em), "seconds": tm, "s_per_sweep_last": f.sweep_seconds[-1], "energy": em[-1],
+                     "unconverged": f.stats["unconverged"], "df64_retries": f.stats["df64_retries"]},
+           "fp64_from_mixed_state": {"sweeps": len(ef), "s_per_sweep_last": g.sweep_seconds[-1], "energy": ef[-1]},
+           "speedup_mixed_vs_fp64_per_sweep": g.sweep_seconds[-1] / f.sweep_seconds[-1],
+           "dE_rel_mixed_vs_fp64": abs(em[-1] - ef[-1]) / abs(ef[-1]),
+           "spectrum_bond": bond, "spectrum_max_abs_diff": float(np.abs(lam_m - lam_f).max()),
+           "spectrum_top5_fp64": lam_f[:5].tolist(), "max_sz_err_mixed_vs_fp64": float(np.abs(sz_m - sz_f).max())}
+    del f, g
+    torch.cuda.empty_cache()
+    return out
+
+
+def tsdrg_rate(n_real: int, with_cpu: bool, n_single: int = 16):
     """Batched tSDRG on `n_real` random-coupling chains J_i = (1-u_i)^(1/delta), u = RandomState(10000+r),
-    n=128, chi=32, delta=1, h=0 (realisations/s), with one realisation of the CPU restatement timed
-    on the host cores beside it."""
+    n=128, chi=32, delta=1, h=0 (realisations/s): all realisations merged in lockstep (one launch
+    of each kernel per merge step for every chain), FP64 and mixed; against one realisation per
+    launch sequence (TSDRG(mpo, chi).run() one after another, FP64) on the first `n_single`
+    realisations, with their kept spectra compared; and the CPU restatement (one realisation)
+    timed on the host cores beside it. The h=0 chain is SU(2) symmetric, so the comparison with
+    the CPU restatement's kept spectra is made on the h=0.5 variant (two realisations)."""
     import torch
 
     import tnpy_gb300 as tg
@@ -242,9 +443,24 @@ def tsdrg_rate(n_real: int, with_cpu: bool):
     bm = tg.BatchedTSDRG(mpos, chi=chi, precision="mixed").run()
     torch.cuda.synchronize()
     dtm = time.perf_counter() - t0
+    ns = min(n_single, n_real)
+    t0 = time.perf_counter()
+    singles = []
+    for r in range(ns):
+        t = tg.TSDRG(mpos[r], chi=chi)
+        t.run()
+        singles.append(t.evals)
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t0
+    diff = max(float(np.abs(np.asarray(singles[r]) - np.asarray(b.evals[r])).max()) for r in range(ns))
+    single_rate = ns / ts
     out = {"workload": f"tsdrg_random_coupling_n{n}_chi{chi}_delta1_h0", "realizations": n_real,
            "value": n_real / dt, "unit": "realizations/s", "precision": "fp64", "seconds": dt,
            "mixed": {"value": n_real / dtm, "seconds": dtm, "e0_realization0": float(bm.evals[0][0])},
+           "one_per_launch_fp64": {"value": single_rate, "realizations": ns, "seconds": ts,
+                                   "max_abs_diff_kept_spectra_vs_batched": diff},
+           "speedup_batched_vs_one_per_launch": (n_real / dt) / single_rate,
+           "speedup_batched_mixed_vs_one_per_launch": (n_real / dtm) / single_rate,
            "e0_realization0": float(b.evals[0][0]),
            "note": "h=0 is SU(2) symmetric: chi=32 cuts through degenerate multiplets, so the kept states "
                    "(and the variational energy) depend on rounding in any implementation"}
@@ -258,6 +474,16 @@ def tsdrg_rate(n_real: int, with_cpu: bool):
         tc = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": 1.0 / tc, "unit": "realizations/s", "cores": os.cpu_count(),
                                "kind": "port", "sample": "one realisation (r=0) of the numpy restatement"}
+        # kept spectra against the one-block-at-a-time FP64 numpy eigh on the h != 0 variant
+        diffs, same = [], True
+        mh = [tg.model.RandomCouplingHeisenberg(n, delta=1.0, h=0.5, seed=10000 + r) for r in range(2)]
+        bh = tg.BatchedTSDRG([x.mpo for x in mh], chi=chi).run()
+        for r, x in enumerate(mh):
+            o = ots.TreeTensorNetworkSDRG(om.random_coupling_heisenberg_mpo(n, x.couplings, fields=x.fields), chi).run()
+            diffs.append(float(np.abs(np.asarray(bh.evals[r]) - o.evals).max()))
+            same = same and [list(q) for q in bh.merges[r]] == [list(q) for q in o.merges]
+        out["parity_h05_vs_cpu_restatement"] = {"realizations": 2, "max_abs_diff_kept_spectra": max(diffs),
+                                                "merge_order_equal": same}
     return out
 
 
@@ -299,14 +525,27 @@ def chains_rate(n_chains: int, with_cpu: bool, workers: int = 16):
 
 # ------------------------------------------------------------------ reference arm
 def run_reference(a):
+    """The reference's CPU path (numpy/scipy restatement; quimb and primme cannot be installed
+    here) on the bench's chain: one step = one real site update of a sweep (see CpuBulkPair),
+    on the machine's host cores with every thread BLAS can use. Untimed set-up builds the seeded
+    random MPS of the GPU arm and converges the bulk pair; then W warm-up and K timed updates."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cb = cpu_sample(a)
+    t_setup = time.perf_counter()
+    pair = CpuBulkPair(*cpu_pair_from_random_mps(a), tol=a.tol)
+    setup_s = time.perf_counter() - t_setup
+    res = cpu_site_updates(pair, a.steps, a.warmup, prepare_s=120.0)
+    cb = cpu_result(a, res, "state: a seeded random MPS whose middle pair has the bench chain's bulk local "
+                            "problem shape (chi x D x chi environments), converged before the warm-up")
+    cb["setup_s"] = setup_s
+    ms = statistics.fmean(res["times"]) * 1e3
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "sweeps/s", "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random MPS, XXZ MPO)",
             "config": workload(a), "cpu_baseline": cb,
+            "step_note": "a step is one site update of the sweep (ms_per_step); value = 1 / (mean site update "
+                         "x sweep_site_weight) sweeps/s",
             "e2e": {"value": cb["value"], "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -411,7 +650,10 @@ def run_ours(a):
     e2e_t = max_over_ranks((time.perf_counter() - t0) / a.steps, dev)
 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    bf16_sust = peaks.get("bf16_tflops_sustained", 1700.0)
+    bf16_sust = peaks.get("bf16_tflops_sustained")
+    peak_src = "of measured"
+    if bf16_sust is None:
+        bf16_sust, peak_src = 1700.0, "of fallback (1.7 PFLOP/s sustained bf16)"
     tf = ROOT / "profiles" / "traffic.txt"
 
     def traffic_of(key):
@@ -422,23 +664,19 @@ def run_ours(a):
                     return float(parts[1])
         return None
 
-    # Ozaki FP64-class GEMM: every launch inside the timed sweeps, CUDA events around each
-    oz_ach = fl_o.value / (ms_o.value / 1e3) / 1e12 if ms_o.value > 0 else None
-    oz_peak = bf16_sust / 36.0
-    roofline_oz = {"kernel": "oz_gemm_kernel (tcgen05 FP64-class GEMM, 36 exact BF16 slice products)",
-                   "bound": "tensor", "achieved": oz_ach, "peak": oz_peak, "unit": "TFLOP/s",
-                   "frac": (oz_ach / oz_peak) if oz_ach else None, "traffic": traffic_of(f"oz_gemm_chi{a.chi}"),
-                   "launches": n_o.value, "kernel_ms_per_sweep": ms_o.value / a.steps,
-                   "share_of_step_time": (ms_o.value / dev_ms) if dev_ms > 0 else None,
-                   "peak_note": "of measured: bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class "
-                                "product); achieved counts algorithmic flops 2*M*N*K over the timed sweeps"}
-    # Other kernel families: one further sweep per family, outside the timed region, with CUDA
-    # events around each launch of that family (library event profiler)
-    fams = {0: "tcgen05 split-BF16 GEMM", 1: "double-FP32 GEMM (QR updates)",
-            3: "QR panel (double-FP32 cluster kernel)", 6: "Ozaki FP64-class GEMM"}
-    shares = {fams[6]: {"launches": n_o.value, "ms_per_sweep": ms_o.value / a.steps,
-                        "share": roofline_oz["share_of_step_time"], "tflops": oz_ach}}
-    prof = {}
+    # Every kernel family of the step: the Ozaki GEMM over the timed sweeps (CUDA events around
+    # each launch, library profiler); the others over one further sweep each, outside the timed
+    # region. The headline roofline is the family with the largest share of the step.
+    fams = {0: ("bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)", 3.0,
+                "bf16_tflops_sustained / 3 (three BF16 products per split-BF16 product)", f"tc_gemm_chi{a.chi}"),
+            1: ("gemm_df64_kernel (double-FP32 SIMT GEMM: QR trailing updates and Q formation)", 36.0,
+                "bf16_tflops_sustained / 36, the FP64-class tensor-core bound the Ozaki GEMM runs against "
+                "(this SIMT kernel does the same FP64-class products on the FP32 pipe)", None),
+            3: ("qrdf::panel_df_kernel (double-FP32 16-CTA cluster Householder panel)", 36.0,
+                "bf16_tflops_sustained / 36 (FP64-class tensor-core bound)", None),
+            6: ("oz_gemm_kernel (tcgen05 FP64-class GEMM, 36 exact BF16 slice products)", 36.0,
+                "bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class product)", f"oz_gemm_chi{a.chi}")}
+    prof = {6: (n_o.value, ms_o.value, fl_o.value, dev_ms, a.steps)}
     for fam in (0, 1, 3):
         lib.tnx_profile_begin(fam)
         sw0, sw1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -448,50 +686,102 @@ def run_ours(a):
         n_f, ms_f, fl_f, by_f = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
         lib.tnx_profile_end(ctypes.byref(n_f), ctypes.byref(ms_f), ctypes.byref(fl_f), ctypes.byref(by_f))
         torch.cuda.synchronize()
-        sweep_ms = sw0.elapsed_time(sw1)
-        prof[fam] = (n_f.value, ms_f.value, fl_f.value, sweep_ms)
-        shares[fams[fam]] = {"launches": n_f.value, "ms_per_sweep": ms_f.value,
-                             "share": ms_f.value / sweep_ms if sweep_ms > 0 else None,
-                             "tflops": fl_f.value / (ms_f.value / 1e3) / 1e12 if ms_f.value > 0 and fl_f.value > 0
-                             else None}
-    n_mv, ms_mv, fl_mv, sweep_mv = prof[0]
-    achieved = fl_mv / (ms_mv / 1e3) / 1e12 if ms_mv > 0 else None
-    peak = bf16_sust / 3.0
-    roofline_mv = {"kernel": "bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)",
-                   "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                   "frac": (achieved / peak) if achieved else None, "traffic": traffic_of(f"tc_gemm_chi{a.chi}"),
-                   "peak_note": "of measured: bf16_tflops_sustained / 3 (three BF16 products per split-BF16 product); "
-                                "achieved counts algorithmic flops 2*M*N*K of the unsplit product, over one "
-                                "profiled sweep after the timed ones",
-                   "launches": n_mv, "kernel_ms_per_sweep": ms_mv,
-                   "share_of_step_time": (ms_mv / sweep_mv) if sweep_mv > 0 else None}
+        prof[fam] = (n_f.value, ms_f.value, fl_f.value, sw0.elapsed_time(sw1), 1)
+
+    def roofline_of(fam):
+        n_l, ms_l, fl_l, sweep_ms, sweeps = prof[fam]
+        name, div, note, tkey = fams[fam]
+        ach = fl_l / (ms_l / 1e3) / 1e12 if ms_l > 0 and fl_l > 0 else None
+        pk = bf16_sust / div
+        return {"kernel": name, "bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                "frac": (ach / pk) if ach else None, "traffic": traffic_of(tkey) if tkey else None,
+                "launches": n_l, "kernel_ms_per_sweep": ms_l / sweeps,
+                "share_of_step_time": (ms_l / sweep_ms) if sweep_ms > 0 else None,
+                "peak_note": f"{peak_src}: {note}; achieved = algorithmic flops (2 M N K per GEMM, "
+                             f"3 m nb^2 per QR panel) / summed CUDA-event time of the family's launches",
+                "window": "the timed sweeps" if fam == 6 else "one profiled sweep after the timed ones"}
+
+    rooflines = {fam: roofline_of(fam) for fam in prof}
+    shares = {fams[f][0].split(" ")[0]: {"launches": r["launches"], "ms_per_sweep": r["kernel_ms_per_sweep"],
+                                         "share": r["share_of_step_time"], "tflops": r["achieved"]}
+              for f, r in rooflines.items()}
+    top = max(rooflines, key=lambda f: rooflines[f]["share_of_step_time"] or 0.0)
+    # the timed-sweep counters of the Davidson: unconverged solves are retried in FP64 and warned
+    dstats = dict(f.stats)
+
+    # time to solution from the seeded random MPS: warm-up sweeps until |dE| < tol
+    conv_at, acc = None, 0.0
+    for k_s, (ts, es) in enumerate(zip(warmup_s, energies)):
+        acc += ts
+        if k_s > 0 and abs(es - energies[k_s - 1]) < a.tol:
+            conv_at = {"sweeps": k_s + 1, "s": acc, "energy": es}
+            break
+
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 (split-bf16 tensor-core matvec, FP64 environments / eigensolver)"
-            if a.precision == "mixed" else "f64",
+            "vs_baseline": None, "dtype": "f64 (split-bf16 tensor-core matvec, FP64-class environments / gauge "
+            "moves, FP64 eigensolver)" if a.precision == "mixed" else "f64",
             "data": "synthetic (seeded random initial MPS, XXZ MPO)", "config": workload(a),
-            "roofline": roofline_oz, "roofline_matvec": roofline_mv, "step_shares": shares, "clocks": clk,
-            "gpu_launches": int(launches),
+            "roofline": rooflines[top], "roofline_ozaki": rooflines[6], "roofline_matvec": rooflines[0],
+            "step_shares": shares, "clocks": clk, "gpu_launches": int(launches),
             "e2e": {"value": world / e2e_t, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d + 8},
             "energy_last": energies[-1], "wall_s_per_step": wall / a.steps,
             "davidson_matvecs_per_site_timed": mv_timed, "launches_before_timed": int(launches0),
-            "warmup_sweeps": {"s": warmup_s, "energy": energies[:a.warmup]}}
-    # CPU restatement: per-site work scaled by the FP64 form's Davidson matvecs on the same state
-    # (the reference's primme call uses the same tol), else by the timed mixed count + the anchor
-    mv_cpu = mv_timed + 1.0
+            "davidson": {"unconverged": dstats["unconverged"], "df64_retries": dstats["df64_retries"],
+                         "iterative_solves": dstats["iterative_solves"], "matvecs": dstats["matvecs"],
+                         "window": "warm-up, timed, e2e and profiled sweeps"},
+            "warmup_sweeps": {"s": warmup_s, "energy": energies[:a.warmup]},
+            "first_sweep_s": warmup_s[0] if warmup_s else None,
+            "time_to_convergence": conv_at}
     if rank == 0 and not a.no_extras:
         line["matvec_forms"] = matvec_forms(f, a.n // 2)
         line["fp64_sweep"] = fp64_sweep(f, dirs[step % 2], a.tol, t_step)
-        mv_cpu = line["fp64_sweep"]["fp64"]["matvecs_per_site"]
+        line["config1"] = config1_line(with_cpu=(world == 1 and not a.no_cpu))
+        line["config2_ramp"] = config2_ramp_line()
+        line["config3"] = config3_line(with_cpu=(world == 1 and not a.no_cpu))
         line["tsdrg"] = tsdrg_rate(a.tsdrg_realizations, with_cpu=(world == 1 and not a.no_cpu))
         line["chains"] = chains_rate(a.chains, with_cpu=(world == 1 and not a.no_cpu))
     if rank == 0 and world == 1 and not a.no_cpu:
-        line["cpu_baseline"] = cpu_sample(a, mv_cpu)
+        line["cpu_baseline"] = cpu_baseline_converged(f, a, dirs[step % 2])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def cpu_baseline_converged(f, a, direction):
+    """CPU restatement timed on the GPU chain's own converged state: the GPU chain sweeps (in
+    `direction`) up to its middle site, the bulk pair there (L_i, R_{i+1}, the two site tensors,
+    their MPO tensors) is copied to the host, the sweep is completed on the GPU, and the CPU
+    restatement performs 2 warm-up and 8 timed site updates on the copy (about 10-20 s)."""
+    import numpy as np
+
+    import tnpy_gb300 as tg
+
+    n = f.n_sites
+    i = n // 2
+    sites = list(range(n - 1)) if direction == tg.Direction.RIGHTWARD else list(range(n - 1, 0, -1))
+
+    def update(site):
+        e, psi = f.one_site_solver(site, a.tol)
+        f.env.update_mps(site, psi)
+        f.perturb_wave_function(site)
+        f.env.split_tensor(site, direction)
+        f.env.update(site, direction)
+
+    k = sites.index(i)
+    for site in sites[:k]:
+        update(site)
+    w = f.env.mpo.device_tensors(f.mps.device)
+    host = lambda t: t.detach().cpu().numpy().astype(np.float64)  # noqa: E731
+    data = (host(f.env.left[i]), host(w[i]), host(w[i + 1]), host(f.env.right[i + 1]),
+            host(f.mps.tensors[i]), host(f.mps.tensors[i + 1]))
+    for site in sites[k:]:
+        update(site)
+    pair = CpuBulkPair(*data, tol=a.tol)
+    res = cpu_site_updates(pair, steps=8, warmup=2)
+    return cpu_result(a, res, "state: the GPU chain's converged bulk pair after the timed sweeps")
 
 
 def main():

@@ -62,6 +62,21 @@ long long tnx_launch_count(void);
 int tnx_profile_begin(int family);
 int tnx_profile_end(int* launches, double* total_ms, double* flops, double* bytes);
 
+/* ---- autotuner ---------------------------------------------------------------------------
+ * Kernel variants are chosen per call site and shape by timing every candidate once on the
+ * caller's stream (first call of that shape, outside stream capture, output-overwriting calls
+ * only) and caching the fastest for the process: the double-FP32 GEMM tile (64 x 128 / 32 x 32),
+ * the FP64-class GEMM engine (tcgen05 Ozaki / double-FP32 SIMT) and the split-BF16 tcgen05 GEMM
+ * tile (128 x 256 / 128 x 128). On by default; TNX_AUTOTUNE=0 in the environment or
+ * tnx_autotune_set(0) keeps the fixed size rules. tnx_autotune_report writes one line per cached
+ * choice, "kind key0..key4 -> variant ms_0 .. ms_(n-1)" (kind 1 / 2 / 3 as listed; -1 ms for a
+ * candidate that did not apply), and returns the bytes needed including the terminating zero.
+ * A builder addition: the reference has no native kernels to tune. */
+int tnx_autotune_set(int enable);
+int tnx_autotune_clear(void);
+int tnx_autotune_count(void);
+size_t tnx_autotune_report(char* buf, size_t len);
+
 /* ---- one-site effective Hamiltonian ------------------------------------------------
  * Replaces Environment.one_site_matvec (tnpy/matrix_product_state.py:411-440):
  *   y[a',s',c'] = sum L[a,w,a'] x[a,s,c] W[w,v,s,s'] R[c,v,c']
@@ -146,6 +161,18 @@ int tnx_eigh_batched(double* A, const int64_t* offsets, const int* sizes, int ba
 size_t tnx_qr_workspace_bytes(int64_t m, int64_t n);
 int tnx_qr(const double* M, int64_t m, int64_t n, double* Q, double* R, void* workspace,
            size_t workspace_bytes, void* stream);
+
+/* Thin SVD of a row-major m x n matrix (m >= n) by one-sided Jacobi in FP64: S (n, descending),
+ * U (m x n, row-major, may be null), VT (n x n, row-major, may be null; V is accumulated only
+ * when VT is given). Replaces np.linalg.svd in linalg.svd (tnpy/linalg.py:9-23) and gives the
+ * Schmidt values of the SVD gauge move (tnpy/matrix_product_state.py:200-223). The singular
+ * values come from the matrix itself (absolute error ~eps * sigma_max, not the
+ * ~sqrt(eps) * sigma_max of a Gram matrix). A column of U whose sigma is exactly zero is left
+ * zero. *sweeps_out (may be null) = Jacobi sweeps run; TNX_ERR_NOT_CONVERGED after 40 sweeps
+ * (results still written). */
+size_t tnx_svd_workspace_bytes(int64_t m, int64_t n, int want_vt);
+int tnx_svd(const double* A, int64_t m, int64_t n, double* S, double* U, double* VT, int* sweeps_out,
+            void* workspace, size_t workspace_bytes, void* stream);
 
 /* One-site gauge move of FiniteDMRG.sweep (tnpy/matrix_product_state.py:187-225,
  * :359-365), QR form: direction = +1: A_site (chi_l d x chi_r) = Q R, A_site <- Q,

@@ -90,7 +90,7 @@ class _FakeSolverSite:
         f = FiniteDMRG.__new__(FiniteDMRG)
         f._exact_solver_dim = 200
         f.max_iter, f.max_basis = 400, 24
-        f.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0, "fp64_retries": 0}
+        f.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0, "df64_retries": 0}
 
         class _Env:
             mps = type("M", (), {"tensors": [torch.zeros((16, 2, 16), dtype=torch.float64)]})()
@@ -102,13 +102,13 @@ class _FakeSolverSite:
         self.f = f
 
 
-def test_unconverged_mixed_solve_is_continued_in_fp64(monkeypatch, caplog):
+def test_unconverged_mixed_solve_is_continued_in_fp64_class(monkeypatch, caplog):
     s = _FakeSolverSite([(-1.0, 0.5, 16, False), (-1.2, 1e-9, 30, True)], monkeypatch)
     s.f.precision = "mixed"
     with caplog.at_level(logging.INFO, logger="tnpy"):
         e, _ = s.f.one_site_solver(0, 1e-8)
-    assert e == -1.2 and s.calls == ["mixed", "fp64"]
-    assert s.f.stats["fp64_retries"] == 1 and s.f.stats["unconverged"] == 0 and s.f.stats["matvecs"] == 46
+    assert e == -1.2 and s.calls == ["mixed", "df64"]
+    assert s.f.stats["df64_retries"] == 1 and s.f.stats["unconverged"] == 0 and s.f.stats["matvecs"] == 46
     assert not any(r.levelno >= logging.WARNING for r in caplog.records)
 
 

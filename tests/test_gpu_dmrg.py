@@ -87,3 +87,34 @@ def test_bond_dimension_ramp(cuda):
     e_ref = o.run(tol=1e-10, max_sweep=12, with_variance=False)[-1]
     assert energies[-1] < e_before - 1e-6
     assert abs(energies[-1] - e_ref) <= 1e-7 * abs(e_ref), (energies[-1], e_ref)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_chi_ramp_with_truncation_error_vs_oracle(cuda, precision):
+    """FiniteDMRG.ramp on XXZ(16, -0.5), chi 4 -> 8 -> 16 (two sweeps per stage, then to
+    convergence): the final energy and middle-bond Schmidt values match the oracle's fixed-chi
+    (16) ground state, and the reported truncation error of the last stage (weight beyond
+    chi = 8) is the oracle state's sum_{j > 8} lambda_j^2."""
+    import tnpy_gb300 as tg
+
+    n = 16
+    mpo = om.xxz_mpo(n, -0.5)
+    f = tg.FiniteDMRG(tg.MatrixProductOperator(mpo), bond_dim=4, seed=5, precision=precision, compute_variance=False)
+    stages = f.ramp([4, 8, 16], sweeps_per_stage=2, tol=1e-11, max_sweep=20)
+    assert [s["chi"] for s in stages] == [4, 8, 16]
+    assert [s["sweeps"] for s in stages][:2] == [2, 2]
+    assert stages[0]["energy"] > stages[1]["energy"] > stages[2]["energy"] - 1e-12
+    assert max(f.mps.bond_dims()) == 16 and f.stats["unconverged"] == 0
+    o = odmrg.FiniteDMRG(mpo, chi=16, seed=5)
+    e_ref = o.run(tol=1e-11, max_sweep=20, with_variance=False)[-1]
+    assert abs(stages[-1]["energy"] - e_ref) <= 1e-9 * abs(e_ref), (stages[-1]["energy"], e_ref)
+    bond = n // 2 - 1
+    psi = o.mps[0]
+    for a in o.mps[1:]:
+        psi = np.tensordot(psi, a, axes=([-1], [0]))
+    psi = psi.reshape(-1) / np.linalg.norm(psi)
+    lam_ref = np.linalg.svd(psi.reshape(2 ** (bond + 1), -1), compute_uv=False)[:16]
+    np.testing.assert_allclose(stages[-1]["spectrum"], lam_ref, atol=1e-7)
+    tr_ref = float(np.sum(lam_ref[8:] ** 2))
+    assert abs(stages[-1]["truncation_error_prev_chi"] - tr_ref) <= 1e-9 + 1e-5 * tr_ref
+    assert stages[1]["truncation_error_prev_chi"] > 0.0 and "truncation_error_prev_chi" not in stages[0]

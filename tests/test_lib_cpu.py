@@ -126,3 +126,38 @@ def test_product_requires_cuda_for_state():
         pytest.skip("CUDA present")
     with pytest.raises(RuntimeError):
         tg.MatrixProductState.random(4, 2, 2)
+
+
+def test_mps_npz_round_trip_and_reference_layout(tmp_path):
+    """MatrixProductState.save / load in .npz (tnpy/matrix_product_state.py:118-168): keys are
+    the site tags I0..I{n-1}, tensors in 'lpr' order with the boundary sites 2-index ((d, chi)
+    and (chi, d)); a file whose keys are in site order, as the reference writes and reads it
+    (:130, :158), loads site by site, and so do more than ten sites (I10 after I9)."""
+    import numpy as np
+    import pytest
+
+    import tnpy_gb300 as tg
+
+    rng = np.random.RandomState(0)
+    n, d = 12, 2
+    dims = [1, 2, 4, 8, 8, 8, 8, 8, 8, 8, 4, 2, 1]
+    arrays = [rng.standard_normal((dims[i], d, dims[i + 1])) for i in range(n)]
+    mps = tg.MatrixProductState(arrays, device="cpu")
+    path = tmp_path / "state.npz"
+    mps.save(str(path))
+    f = np.load(str(path))
+    assert list(f.files) == [f"I{s}" for s in range(n)]
+    assert f["I0"].shape == (d, 2) and f[f"I{n - 1}"].shape == (2, d) and f["I5"].shape == (8, d, 8)
+    back = tg.MatrixProductState.load(str(path), device="cpu")
+    for a, b in zip(arrays, back.tensors):
+        np.testing.assert_array_equal(a, b.numpy())
+    # a reference-written file: site tags in site order, boundary tensors 2-index
+    ref = tmp_path / "ref.npz"
+    np.savez(str(ref), **{f"I{s}": (a[0] if s == 0 else a[:, :, 0] if s == n - 1 else a) for s, a in enumerate(arrays)})
+    back2 = tg.MatrixProductState.load(str(ref), device="cpu")
+    for a, b in zip(arrays, back2.tensors):
+        np.testing.assert_array_equal(a, b.numpy())
+    with pytest.raises(ValueError):
+        mps.save(str(tmp_path / "state.txt"))
+    with pytest.raises(ValueError):
+        tg.MatrixProductState.load(str(tmp_path / "state.hdf"))

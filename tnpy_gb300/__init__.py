@@ -14,7 +14,7 @@ if not logger.handlers:
 logger.setLevel(logging.WARNING)
 
 from . import _lib  # noqa: E402  (fails loudly when libtnx.so is missing)
-from . import linalg, model  # noqa: E402
+from . import autotune, linalg, model  # noqa: E402
 from .finite_dmrg import BatchedFiniteDMRG, FiniteDMRG, Metric  # noqa: E402
 from .matrix_product_state import (  # noqa: E402
     Direction,

@@ -77,6 +77,12 @@ SIGNATURES = {
     "tnx_tsdrg_project": (_int, [_vp, _vp, _vp, _vp, _int, _vp, _int, _int, _int, _int, _vp]),
     "tnx_tsdrg_block_eigh_workspace_bytes": (_sz, [_int, _int, _int, _int]),
     "tnx_tsdrg_block_eigh": (_int, [_vp, _vp, _vp, _int, _int, _int, _int, _int, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "tnx_autotune_set": (_int, [_int]),
+    "tnx_autotune_clear": (_int, []),
+    "tnx_autotune_count": (_int, []),
+    "tnx_autotune_report": (_sz, [_c.c_char_p, _sz]),
+    "tnx_svd_workspace_bytes": (_sz, [_i64, _i64, _int]),
+    "tnx_svd": (_int, [_vp, _i64, _i64, _vp, _vp, _vp, _pi, _vp, _sz, _vp]),
     "tnx_gemm_f64": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _i64, _vp, _i64, _i64, _dbl,
                             _vp, _i64, _i64, _i64, _vp]),
 }

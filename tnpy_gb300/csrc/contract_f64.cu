@@ -278,8 +278,15 @@ bool use_oz(int64_t m, int64_t n, int64_t k) {
 int gemm_fp64_class_oz(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                        int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* oz_ws,
                        size_t oz_bytes, cudaStream_t st) {
-  if (df && oz_ws && use_oz(m, n, k) && oz_bytes >= gemm_oz_workspace_bytes(m, n, k))
-    return gemm_oz(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, oz_ws, oz_bytes, st);
+  if (df && oz_ws && use_oz(m, n, k) && oz_bytes >= gemm_oz_workspace_bytes(m, n, k)) {
+    // FP64-class engine, autotuned per shape: 0 tcgen05 Ozaki GEMM, 1 double-FP32 SIMT GEMM
+    auto run = [&](int v) -> int {
+      if (v == 0) return gemm_oz(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, oz_ws, oz_bytes, st);
+      return gemm_fp64_class(true, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+    };
+    const TuneKey key{2, int64_t(ta) * 2 + int64_t(tb), m, n, k, 0};
+    return autotuned(key, 2, 0, beta == 0.0, st, run);
+  }
   return gemm_fp64_class(df, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
 }
 

@@ -543,14 +543,15 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // Stagnation: the split-BF16 operand is not exactly symmetric, so the residual of the
   // mixed operator stops falling at ~1e-5 |H| (its rounding floor). The first phase treats
   // "no 10% gain within `patience` matvecs" as that floor only when the residual is already
-  // within ~100x of it (below 1e-3 |H|); further out a Davidson residual can plateau while
-  // theta still falls (hard starts, small local gaps), and the phase keeps expanding, with
-  // GD+1 restarts, until max_iter. The FP64 forms treat stagnation as their floor below
-  // 1e-11 |H| (tol = 0 asks for machine accuracy, as primme's default does).
+  // within ~10x of it (below 1e-4 |H|); further out a Davidson residual can plateau for tens of
+  // matvecs while theta still falls (hard starts of a first sweep, small local gaps), and the
+  // phase keeps expanding, with GD+1 restarts, until max_iter. The FP64 forms treat
+  // stagnation as their floor below 1e-11 |H| (tol = 0 asks for machine accuracy, as primme's
+  // default does).
   double best = INFINITY;
   int best_it = 0;
   const int patience = mixed ? 8 : 40;
-  const double mixed_floor_band = 1e-3, fp64_floor_band = 1e-11;
+  const double mixed_floor_band = 1e-4, fp64_floor_band = 1e-11;
   // The mixed form hands over to the anchored phase once the split-BF16 residual is below
   // 3e-6 |theta| or has stagnated at its ~1e-5 |H| floor (an earlier hand-over can leave the
   // solve on an excited state), and then converges the FP64-class residual to
@@ -675,7 +676,9 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
           best = rnorm;
           best_it = iters;
         } else if (iters - best_it >= patience) {
-          break;
+          if (near || rnorm <= mixed_floor_band * hscale()) break;  // at the floor: a fresh anchor
+          best = rnorm;  // a plateau far above the floor: keep the subspace and expand
+          best_it = iters;
         }
         if (iters >= max_iter) break;
         if (k == mb) {

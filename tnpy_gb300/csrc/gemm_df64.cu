@@ -160,27 +160,36 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
     return e ? atoi(e) : 2;
   }();
   const int64_t big = ((n + 127) / 128) * ((m + 63) / 64) * batch;
-  const bool small = big < int64_t(small_waves) * 152;
-  const int64_t bm = small ? 32 : 64, bn = small ? 32 : 128;
-  dim3 grid((unsigned)((n + bn - 1) / bn), (unsigned)((m + bm - 1) / bm), (unsigned)batch);
-  TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_df64: m too large");
+  const bool small_rule = big < int64_t(small_waves) * 152;
+  // variant 0: 64 x 128 tiles, 256 threads; variant 1: 32 x 32 tiles, 64 threads
+  auto launch = [&](int v) -> int {
+    const bool small = v == 1;
+    const int64_t bm = small ? 32 : 64, bn = small ? 32 : 128;
+    dim3 grid((unsigned)((n + bn - 1) / bn), (unsigned)((m + bm - 1) / bm), (unsigned)batch);
+    TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_df64: m too large");
+    auto go = [&](auto kernel, int nt) {
+      kernel<<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+    };
+    if (small) {
+      if (!ta && !tb) go(gemm_df64_kernel<false, false, 32, 32, 64>, 64);
+      else if (ta && !tb) go(gemm_df64_kernel<true, false, 32, 32, 64>, 64);
+      else if (!ta && tb) go(gemm_df64_kernel<false, true, 32, 32, 64>, 64);
+      else go(gemm_df64_kernel<true, true, 32, 32, 64>, 64);
+    } else {
+      if (!ta && !tb) go(gemm_df64_kernel<false, false, 64, 128, 256>, 256);
+      else if (ta && !tb) go(gemm_df64_kernel<true, false, 64, 128, 256>, 256);
+      else if (!ta && tb) go(gemm_df64_kernel<false, true, 64, 128, 256>, 256);
+      else go(gemm_df64_kernel<true, true, 64, 128, 256>, 256);
+    }
+    TNX_LAUNCH_CHECK();
+    return TNX_OK;
+  };
   profile_mark(KF_F64_GEMM, st, true);
-  auto go = [&](auto kernel, int nt) { kernel<<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total); };
-  if (small) {
-    if (!ta && !tb) go(gemm_df64_kernel<false, false, 32, 32, 64>, 64);
-    else if (ta && !tb) go(gemm_df64_kernel<true, false, 32, 32, 64>, 64);
-    else if (!ta && tb) go(gemm_df64_kernel<false, true, 32, 32, 64>, 64);
-    else go(gemm_df64_kernel<true, true, 32, 32, 64>, 64);
-  } else {
-    if (!ta && !tb) go(gemm_df64_kernel<false, false, 64, 128, 256>, 256);
-    else if (ta && !tb) go(gemm_df64_kernel<true, false, 64, 128, 256>, 256);
-    else if (!ta && tb) go(gemm_df64_kernel<false, true, 64, 128, 256>, 256);
-    else go(gemm_df64_kernel<true, true, 64, 128, 256>, 256);
-  }
+  const TuneKey key{1, int64_t(ta) * 2 + int64_t(tb), m, n, k_total > 0 ? k_total : k, batch};
+  TNX_TRY(autotuned(key, 2, small_rule ? 1 : 0, beta == 0.0, st, launch));
   profile_mark(KF_F64_GEMM, st, false);
   profile_work(KF_F64_GEMM, 2.0 * double(m) * n * (k_total > 0 ? k_total : k * batch),
                8.0 * (double(m) * k + double(k) * n + double(m) * n) * batch);
-  TNX_LAUNCH_CHECK();
   return TNX_OK;
 }
 

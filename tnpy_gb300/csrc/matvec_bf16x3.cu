@@ -418,13 +418,17 @@ int mixed_apply_t(const double* W, const T* x, T* y, int64_t chi_l, int64_t d, i
   // B1[(s c)][a] = x[a][(s c)]
   split_transpose_kernel<T><<<tgrid(m.K1p, m.N1), tb, 0, st>>>(x, chi_l, m.N1, m.b1h, m.b1l, m.K1p);
   TNX_LAUNCH_CHECK();
-  // step 1: T1 (FP32) = A1 . B1^T
-  if (m.N1 >= 256)
-    TNX_TRY(launch_gemm<256>(m.a1h, m.a1l, m.b1h, m.b1l, int(m.M1), int(m.N1), int(m.K1p), m.T1, m.N1, false,
-                             m.flag, st, chi_l));
-  else
-    TNX_TRY(launch_gemm<128>(m.a1h, m.a1l, m.b1h, m.b1l, int(m.M1), int(m.N1), int(m.K1p), m.T1, m.N1, false,
-                             m.flag, st, chi_l));
+  // step 1: T1 (FP32) = A1 . B1^T; 128 x 256 or 128 x 128 tiles, autotuned per shape
+  {
+    auto run = [&](int v) -> int {
+      if (v == 0)
+        return launch_gemm<256>(m.a1h, m.a1l, m.b1h, m.b1l, int(m.M1), int(m.N1), int(m.K1p), m.T1, m.N1, false,
+                                m.flag, st, chi_l);
+      return launch_gemm<128>(m.a1h, m.a1l, m.b1h, m.b1l, int(m.M1), int(m.N1), int(m.K1p), m.T1, m.N1, false,
+                              m.flag, st, chi_l);
+    };
+    TNX_TRY(autotuned(TuneKey{3, m.M1, m.N1, m.K1p, 0, 0}, 2, m.N1 >= 256 ? 0 : 1, m.N1 >= 256, st, run));
+  }
   // step 2: MPO contraction into the split A3 operand
   {
     int64_t total = chi_l * chi_r;
@@ -435,9 +439,17 @@ int mixed_apply_t(const double* W, const T* x, T* y, int64_t chi_l, int64_t d, i
                                                                  int(dl), int(dr), m.K3p);
     TNX_LAUNCH_CHECK();
   }
-  // step 3: y = A3 . B3^T (FP32 accumulators written as T)
-  TNX_TRY(launch_gemm<128>(m.a3h, m.a3l, m.b3h, m.b3l, int(m.M3), int(m.N3), int(m.K3p), y, m.N3,
-                           sizeof(T) == 8, m.flag, st, chi_r * dr));
+  // step 3: y = A3 . B3^T (FP32 accumulators written as T); tiles autotuned per shape
+  {
+    auto run = [&](int v) -> int {
+      if (v == 0)
+        return launch_gemm<256>(m.a3h, m.a3l, m.b3h, m.b3l, int(m.M3), int(m.N3), int(m.K3p), y, m.N3,
+                                sizeof(T) == 8, m.flag, st, chi_r * dr);
+      return launch_gemm<128>(m.a3h, m.a3l, m.b3h, m.b3l, int(m.M3), int(m.N3), int(m.K3p), y, m.N3,
+                              sizeof(T) == 8, m.flag, st, chi_r * dr);
+    };
+    TNX_TRY(autotuned(TuneKey{3, m.M3, m.N3, m.K3p, int64_t(sizeof(T)), 0}, 2, 1, m.N3 >= 256, st, run));
+  }
   return TNX_OK;
 }
 

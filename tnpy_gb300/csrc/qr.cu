@@ -620,6 +620,10 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
                      : launch_panel<32, 8, false>(F, m, j0, nb, tau, T, st);
   }
   profile_mark(KF_QR_PANEL, st, false);
+  // algorithmic work of a Householder panel of nb columns over the m - j0 remaining rows:
+  // 2 (m - j0) nb^2 - 2 nb^3 / 3 flops, plus nb^2 (m - j0) for the T factor
+  const double mr = double(m - j0), b = double(nb);
+  profile_work(KF_QR_PANEL, 3.0 * mr * b * b - 2.0 * b * b * b / 3.0, 8.0 * mr * b * 2.0);
   return rc;
 }
 

@@ -3,9 +3,11 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 
 #include "../../include/tnx.h"
 
@@ -54,6 +56,29 @@ bool profiling(int family);
 void profile_mark(int family, cudaStream_t st, bool start);
 // algorithmic work (flops, bytes) of the launch just marked, summed while profiling
 void profile_work(int family, double flops, double bytes);
+
+// ---- autotuner (autotune.cu) -------------------------------------------------------------
+// Key: {kind, shape...}; kind 1 double-FP32 GEMM tile, 2 FP64-class GEMM engine, 3 split-BF16
+// tcgen05 GEMM tile. autotune_choose returns (in *choice) the cached variant for key, or times
+// run(0..nv-1) once each on st, caches the fastest and leaves its output in place (*ran = true);
+// `fallback` when tuning is off, the stream is capturing, or no candidate ran (*ran = false:
+// the caller launches *choice itself). run(v) must overwrite the same outputs for every v.
+using TuneKey = std::array<int64_t, 6>;
+constexpr int kTuneMaxVariants = 4;
+bool autotune_enabled();
+int autotune_choose(const TuneKey& key, int nv, int fallback, cudaStream_t st, const std::function<int(int)>& run,
+                    int* choice, bool* ran);
+// tuned launch: the chosen variant's output is in place on return
+inline int autotuned(const TuneKey& key, int nv, int fallback, bool tunable, cudaStream_t st,
+                     const std::function<int(int)>& run) {
+  int choice = fallback;
+  bool ran = false;
+  if (tunable) {
+    const int rc = autotune_choose(key, nv, fallback, st, run, &choice, &ran);
+    if (rc != TNX_OK) return rc;
+  }
+  return ran ? TNX_OK : run(choice);
+}
 
 #define TNX_TRY(call)                     \
   do {                                    \

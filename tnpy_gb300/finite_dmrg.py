@@ -59,6 +59,7 @@ class FiniteDMRG:
         max_basis: int = 24,
         compute_variance: bool = True,
         device=None,
+        env_precision: str = "fp64",
     ):
         if bond_dim is None:
             bond_dim = chi
@@ -78,12 +79,15 @@ class FiniteDMRG:
         self.compute_variance = compute_variance
         if mps is None:
             mps = MatrixProductState.random(self._n_sites, self._bond_dim, self._phys_dim, seed=seed, device=device)
-        self._env = Environment(mpo=mpo, mps=mps, precision=precision)
+        env_dtypes = {"fp64": torch.float64, "fp32": torch.float32}
+        if env_precision not in env_dtypes:
+            raise ValueError(f"env_precision must be 'fp64' or 'fp32', not {env_precision!r}")
+        self._env = Environment(mpo=mpo, mps=mps, precision=precision, env_dtype=env_dtypes[env_precision])
         self._energies = [np.nan]
         self._variances = [np.nan]
         self.sweep_seconds: list[float] = []
         self.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0,
-                      "fp64_retries": 0}
+                      "df64_retries": 0}
 
     # ---- properties (finite_dmrg.py:78-95) ----------------------------------------------
     @property
@@ -122,8 +126,9 @@ class FiniteDMRG:
 
         An iterative solve that ends without meeting ``tol`` is never passed on silently (the
         reference's primme.eigsh raises on non-convergence by default): a mixed-precision
-        solve is first continued by the FP64 Davidson from the vector it reached
-        (``stats['fp64_retries']``); a solve that still fails is logged as a warning on the
+        solve is first continued by the FP64-class Davidson ('df64': Ozaki-sliced FP64 products
+        on the tensor cores) from the vector it reached (``stats['df64_retries']``); a solve
+        that still fails is logged as a warning on the
         ``tnpy`` logger and counted in ``stats['unconverged']``, or raises RuntimeError with
         ``raise_on_fail=True``."""
         x = self.mps.tensors[site]
@@ -141,12 +146,12 @@ class FiniteDMRG:
         e, rn, its, ok = K.davidson1(L, W, R, psi, tol=tol, max_iter=max_iter, max_basis=max_basis,
                                      precision=precision)
         self.stats["matvecs"] += its
-        if not ok and K.precision_code(precision) != K.precision_code("fp64"):
-            self.stats["fp64_retries"] += 1
+        if not ok and K.precision_code(precision) == K.precision_code("mixed"):
+            self.stats["df64_retries"] += 1
             logger.info(f"site {site}: {precision} Davidson stopped at residual {rn:.3e} after {its} matvecs; "
-                        f"continuing in FP64")
+                        f"continuing in FP64-class arithmetic")
             e, rn, its, ok = K.davidson1(L, W, R, psi, tol=tol, max_iter=max_iter, max_basis=max_basis,
-                                         precision="fp64")
+                                         precision="df64")
             self.stats["matvecs"] += its
         if not ok:
             self.stats["unconverged"] += 1
@@ -166,6 +171,52 @@ class FiniteDMRG:
         self.mps.enlarge_bond_dim(new_bond_dim, seed=seed)
         self._bond_dim = int(new_bond_dim)
         self._env.rebuild()
+
+    def ramp(self, bond_dims, sweeps_per_stage: int = 2, tol: float = 1e-8, max_sweep: int = 20,
+             bond: int | None = None, **kwargs) -> list[dict]:
+        """Bond-dimension ramp (a builder addition: the reference fixes the bond dimension of its
+        one-site DMRG, finite_dmrg.py:113-114 and matrix_product_state.py:227-228 are stubs).
+
+        For each chi in ``bond_dims`` the MPS is grown to chi (``enlarge_bond_dim``, the state
+        unchanged) and swept: ``sweeps_per_stage`` sweeps (rounded up to an even number, so that
+        a stage ends leftward with the centre on site 0, where the next enlargement needs it),
+        and on the last stage until |dE| < tol after a leftward sweep or ``max_sweep`` sweeps.
+        After each stage the Schmidt values on ``bond`` (default: the middle bond) are computed
+        by a direct FP64 SVD. The truncation error of stage k is the weight its state would
+        lose at that bond if cut back to the previous stage's chi, sum_{j > chi_(k-1)} lambda_j^2:
+        the discarded weight a chi_(k-1) calculation commits there, as measured by the larger
+        state (the last stage reports the smallest kept weight lambda_chi^2 beside it).
+        Returns one dict per stage: chi, sweeps, energy, seconds, spectrum (host array),
+        truncation_error_prev_chi and smallest_kept_weight."""
+        bond = self.n_sites // 2 - 1 if bond is None else int(bond)
+        stages: list[dict] = []
+        per = sweeps_per_stage + (sweeps_per_stage % 2)
+        for k, chi in enumerate(bond_dims):
+            if chi != self.bond_dim:
+                self.enlarge_bond_dim(int(chi))
+            last = k == len(bond_dims) - 1
+            n_sw = max_sweep if last else per
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            es: list[float] = []
+            for j in range(n_sw):
+                direction = Direction.RIGHTWARD if j % 2 == 0 else Direction.LEFTWARD
+                e = self.sweep(direction, tol=tol, **kwargs)
+                es.append(e)
+                self._energies.append(e)
+                self._variances.append(np.nan)
+                if last and j % 2 == 1 and len(es) >= 2 and abs(es[-1] - es[-2]) < tol:
+                    break
+            torch.cuda.synchronize()
+            lam = MatrixProductStateMeasurements(self.mps).entanglement_spectrum(bond)
+            stage = {"chi": int(chi), "sweeps": len(es), "energy": es[-1], "energies": es,
+                     "seconds": time.perf_counter() - t0, "spectrum": lam,
+                     "smallest_kept_weight": float(lam[-1] ** 2)}
+            if stages:
+                prev = stages[-1]["chi"]
+                stage["truncation_error_prev_chi"] = float(np.sum(lam[prev:] ** 2))
+            stages.append(stage)
+        return stages
 
     def perturb_wave_function(self, site: int, alpha: float = 1e-5):
         """psi += alpha H_eff psi, in place, not renormalised (finite_dmrg.py:116-141)."""

@@ -175,6 +175,23 @@ def qr(M: torch.Tensor):
     return Q, Rm
 
 
+def svd(M: torch.Tensor, want_u: bool = True, want_vt: bool = True):
+    """Thin SVD of an m x n (m >= n) matrix by one-sided Jacobi (tnx_svd): (U, S, VT), S
+    descending; U / VT are None when not requested."""
+    M = _f64(M, "matrix")
+    m, n = M.shape
+    if m < n:
+        raise ValueError(f"svd needs m >= n (got {m} x {n})")
+    S = torch.empty(n, dtype=torch.float64, device=M.device)
+    U = torch.empty((m, n), dtype=torch.float64, device=M.device) if want_u else None
+    VT = torch.empty((n, n), dtype=torch.float64, device=M.device) if want_vt else None
+    wp, wn = Workspace.get(lib.tnx_svd_workspace_bytes(m, n, int(want_vt)), M.device)
+    sweeps = ctypes.c_int(0)
+    check("tnx_svd", lib.tnx_svd(ptr(M), m, n, ptr(S), ptr(U), ptr(VT), ctypes.byref(sweeps), wp, wn,
+                                 stream_ptr()))
+    return U, S, VT
+
+
 def gauge_move(direction: int, a_site: torch.Tensor, a_nb: torch.Tensor, precision="fp64"):
     """In-place one-site gauge move (QR form of split_tensor, matrix_product_state.py:187-225)."""
     if not (a_site.is_contiguous() and a_nb.is_contiguous()):

@@ -55,25 +55,36 @@ def eigh(matrix, k: int = 1, backend: str = "numpy", **kwargs):
 
 
 def svd(matrix, cutoff: int):
-    """Reduced SVD sliced to ``cutoff`` (linalg.py:9-23): Householder QR followed by the
-    Jacobi eigensolver on R R^T (singular values to ~eps*s_max absolute accuracy)."""
+    """Reduced SVD sliced to ``cutoff`` (linalg.py:9-23): Householder QR (M = Q R) and a
+    one-sided Jacobi SVD of R (R = U_r S V^T) on the device, U = Q U_r, all in FP64. The singular
+    values come from R itself, so a small singular value keeps an absolute error of
+    ~eps * s_max (a Gram matrix R R^T would leave ~sqrt(eps) * s_max), and U, V^T are orthonormal
+    to working accuracy. Columns of U whose singular value is exactly zero are completed to an
+    orthonormal set (np.linalg.svd does the same)."""
     m = _dev(matrix)
     rows, cols = m.shape
     if rows < cols:
         u, s, vt = svd(m.T.contiguous(), cutoff)
         return vt.T.contiguous(), s, u.T.contiguous()
     q, r = K.qr(m)  # m = Q R, R cols x cols
-    g = K.gemm(r, r, trans_b=True)  # R R^T
-    g = 0.5 * (g + g.T)
-    w, ur = K.eigh_batched([g.contiguous()], keep=cols)
-    w, ur = w[0].flip(0), ur[0].flip(1)
-    s = w.clamp_min(0.0).sqrt()
-    u = K.gemm(q, ur.contiguous())
-    # V^T = S^-1 U_r^T R for non-zero singular values
-    vt = K.gemm(ur.contiguous(), r, trans_a=True)
-    safe = torch.where(s > 0, s, torch.ones_like(s))
-    vt = vt / safe[:, None]
+    ur, s, vt = K.svd(r)
+    u = K.gemm(q, ur)
+    zero = (s == 0).nonzero().flatten()
+    if zero.numel():
+        u = _complete_columns(u, zero)
     return u[:, :cutoff].contiguous(), s[:cutoff].contiguous(), vt[:cutoff, :].contiguous()
+
+
+def _complete_columns(u: torch.Tensor, cols: torch.Tensor) -> torch.Tensor:
+    """Replace the given (zero) columns of u, whose other columns are orthonormal, by unit
+    vectors orthogonal to everything else: seeded random fill, Householder QR, signs of the
+    kept columns restored from diag(R)."""
+    g = torch.Generator(device="cpu").manual_seed(0)
+    u = u.clone()
+    u[:, cols] = torch.randn((u.shape[0], cols.numel()), generator=g, dtype=torch.float64).to(u.device)
+    q, r = K.qr(u.contiguous())
+    sign = torch.where(torch.diagonal(r) < 0, -1.0, 1.0).to(torch.float64)
+    return (q * sign[None, :]).contiguous()
 
 
 def eigshmv(linear_operator, v0, k: int = 1, which: str = "SA", tol: float = 0, **kwargs):

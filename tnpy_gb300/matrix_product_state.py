@@ -216,38 +216,52 @@ class OneSiteOperator:
 
 
 class Environment:
-    def __init__(self, mpo: MatrixProductOperator, mps: MatrixProductState, precision="fp64"):
+    def __init__(self, mpo: MatrixProductOperator, mps: MatrixProductState, precision="fp64",
+                 env_dtype: torch.dtype = torch.float64):
         """Left / right environments of ``mps`` under ``mpo`` (matrix_product_state.py:231-250).
 
         ``precision`` selects the contraction kernels of the environment updates and gauge
-        moves: 'fp64' native FP64; 'mixed' (and 'df64') FP64-class double-FP32 arithmetic."""
+        moves: 'fp64' native FP64; 'mixed' (and 'df64') FP64-class arithmetic. ``env_dtype``
+        is the storage type of the environments: float64, or float32 (half the resident
+        bytes; each environment is computed in the contraction's arithmetic and rounded to
+        FP32 when stored, and widened back to FP64 when a site's operator is read)."""
         if mpo.n_sites != mps.n_sites:
             raise ValueError("MPO and MPS sizes differ")
+        if env_dtype not in (torch.float64, torch.float32):
+            raise ValueError(f"environments are stored as float64 or float32, not {env_dtype}")
         self._mpo = mpo
         self._mps = mps
         self._n_sites = mps.n_sites
         self._w = mpo.device_tensors(mps.device)
         self.precision = precision
-        one = torch.ones((1, 1, 1), dtype=torch.float64, device=mps.device)
-        self._left: dict[int, torch.Tensor] = {0: one}
-        self._right: dict[int, torch.Tensor] = {self._n_sites - 1: one.clone()}
-        for site in range(1, self._n_sites):
-            self.update_left(site)
-        for site in range(self._n_sites - 2, -1, -1):
-            self.update_right(site)
+        self.env_dtype = env_dtype
+        self.rebuild()
 
     def close(self):
         del self._left, self._right
 
     def rebuild(self):
         """Recompute every environment (after the bond dimensions changed)."""
-        one = torch.ones((1, 1, 1), dtype=torch.float64, device=self._mps.device)
+        one = torch.ones((1, 1, 1), dtype=self.env_dtype, device=self._mps.device)
         self._left = {0: one}
         self._right = {self._n_sites - 1: one.clone()}
         for site in range(1, self._n_sites):
             self.update_left(site)
         for site in range(self._n_sites - 2, -1, -1):
             self.update_right(site)
+
+    def _f64(self, t: torch.Tensor) -> torch.Tensor:
+        return t if t.dtype == torch.float64 else t.to(torch.float64)
+
+    def _store(self, store: dict, site: int, e: torch.Tensor):
+        if self.env_dtype == torch.float64:
+            store[site] = e
+        else:
+            old = store.get(site)
+            if old is not None and old.shape == e.shape:
+                old.copy_(e)
+            else:
+                store[site] = e.to(self.env_dtype)
 
     @property
     def mpo(self) -> MatrixProductOperator:
@@ -272,22 +286,24 @@ class Environment:
     def update_left(self, site: int):
         """L_site from L_{site-1}, A_{site-1}, W_{site-1} (:296-315)."""
         a = self._mps.tensors[site - 1]
-        out = self._left.get(site)
+        out = self._left.get(site) if self.env_dtype == torch.float64 else None
         shape = (a.shape[2], self._w[site - 1].shape[1], a.shape[2])
         if out is None or tuple(out.shape) != shape:
             out = None
-        self._left[site] = K.env_update(1, self._left[site - 1], a, self._w[site - 1], out=out,
-                                        precision=self.precision)
+        e = K.env_update(1, self._f64(self._left[site - 1]), a, self._w[site - 1], out=out,
+                         precision=self.precision)
+        self._store(self._left, site, e)
 
     def update_right(self, site: int):
         """R_site from R_{site+1}, A_{site+1}, W_{site+1} (:317-336)."""
         a = self._mps.tensors[site + 1]
-        out = self._right.get(site)
+        out = self._right.get(site) if self.env_dtype == torch.float64 else None
         shape = (a.shape[0], self._w[site + 1].shape[0], a.shape[0])
         if out is None or tuple(out.shape) != shape:
             out = None
-        self._right[site] = K.env_update(-1, self._right[site + 1], a, self._w[site + 1], out=out,
-                                         precision=self.precision)
+        e = K.env_update(-1, self._f64(self._right[site + 1]), a, self._w[site + 1], out=out,
+                         precision=self.precision)
+        self._store(self._right, site, e)
 
     def update(self, site: int, direction: Direction):
         """:338-353."""
@@ -308,15 +324,16 @@ class Environment:
 
     def one_site_full_matrix(self, site: int) -> torch.Tensor:
         """Dense H_eff, rows = ket (:372-409)."""
-        return K.full_matrix1(self._left[site], self._w[site], self._right[site])
+        return K.full_matrix1(self._f64(self._left[site]), self._w[site], self._f64(self._right[site]))
 
     def one_site_matvec(self, site: int, precision=None) -> OneSiteOperator:
-        return OneSiteOperator(self._left[site], self._w[site], self._right[site],
+        return OneSiteOperator(self._f64(self._left[site]), self._w[site], self._f64(self._right[site]),
                                tuple(self._mps.tensors[site].shape),
                                precision=precision or "fp64")
 
     def site_operator(self, site: int):
-        return self._left[site], self._w[site], self._right[site]
+        """(L, W, R) of ``site`` as FP64 device tensors."""
+        return self._f64(self._left[site]), self._w[site], self._f64(self._right[site])
 
     def variance(self) -> float:
         """<H^2> - <H>^2 on the current (unnormalised) MPS (:367-370)."""
@@ -370,27 +387,33 @@ class MatrixProductStateMeasurements:
             out[i] = torch.dot(a.reshape(-1), K.matvec1(lefts[i], sz, rights[i], a).reshape(-1))
         return (out / nrm).cpu().numpy()
 
-    def entanglement_spectrum(self, bond: int) -> np.ndarray:
-        """Singular values on ``bond`` (between sites bond and bond+1), largest first, for a
-        normalised state: eigenvalues of the reduced density matrix rho = L_norm^(1/2) ...
-        computed as the eigenvalues of G_L^(1/2) G_R G_L^(1/2) with the norm environments
-        G_L (sites <= bond) and G_R (sites > bond)."""
+    def schmidt_values(self, bond: int) -> torch.Tensor:
+        """Schmidt values on ``bond`` (between sites bond and bond+1) of the normalised state,
+        largest first, as a device tensor. A copy of the MPS is gauged with the orthogonality
+        centre on site ``bond`` (Householder QR moves from both ends, FP64), and the singular
+        values of the centre tensor reshaped to (chi_l d, chi_r) are computed directly by
+        Householder QR and a one-sided Jacobi SVD of R: the singular values of the SVD gauge
+        move (matrix_product_state.py:200-223) at that bond. No Gram matrix is formed, so the
+        small values keep an absolute error of ~eps * s_max."""
         mps = self._mps
-        d, dev = mps.phys_dim, mps.device
-        eye = torch.eye(d, dtype=torch.float64, device=dev).reshape(1, 1, d, d).contiguous()
-        gl = torch.ones((1, 1, 1), dtype=torch.float64, device=dev)
-        for a in mps.tensors[: bond + 1]:
-            gl = K.env_update(1, gl, a, eye)
-        gr = torch.ones((1, 1, 1), dtype=torch.float64, device=dev)
-        for a in mps.tensors[:bond:-1]:
-            gr = K.env_update(-1, gr, a, eye)
-        gl, gr = gl[:, 0, :], gr[:, 0, :]
-        # rho's spectrum = eig(G_L G_R) (similar to G_L^1/2 G_R G_L^1/2, both symmetric PSD)
-        from . import linalg
+        n = mps.n_sites
+        if not 0 <= bond < n - 1:
+            raise ValueError(f"bond {bond} is not between two sites of a {n}-site chain")
+        t = [a.clone() for a in mps.tensors]
+        for site in range(bond):
+            K.gauge_move(1, t[site], t[site + 1])
+        for site in range(n - 1, bond, -1):
+            K.gauge_move(-1, t[site], t[site - 1])
+        c = t[bond]
+        cl, d, cr = c.shape
+        m = c.reshape(cl * d, cr)
+        if m.shape[0] < m.shape[1]:
+            m = m.T.contiguous()
+        _, r = K.qr(m)
+        _, sv, _ = K.svd(r, want_u=False, want_vt=False)
+        return sv / torch.linalg.vector_norm(sv)
 
-        wl, vl = linalg.eigh(0.5 * (gl + gl.T), k=gl.shape[0])
-        sq = vl * wl.clamp_min(0).sqrt()[None, :]
-        m = sq.T @ gr @ sq
-        w, _ = linalg.eigh(0.5 * (m + m.T), k=m.shape[0])
-        w = w.clamp_min(0) / w.clamp_min(0).sum()
-        return torch.flip(w.sqrt(), [0]).cpu().numpy()
+    def entanglement_spectrum(self, bond: int) -> np.ndarray:
+        """Schmidt values on ``bond`` (``schmidt_values``) as a host array: the entanglement
+        spectrum's lambda_k, with sum lambda_k^2 = 1."""
+        return self.schmidt_values(bond).cpu().numpy()
