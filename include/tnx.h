@@ -185,6 +185,51 @@ int tnx_gauge_move(int direction, double* A_site, double* A_neighbour, int64_t c
                    int64_t d, int64_t chi_r, int64_t chi_other, int precision, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* ---- many chains in lockstep ------------------------------------------------------------
+ * Independent chains of one shape (equal bonds, MPO bond and physical dimension) stacked with
+ * a fixed stride between chains (sX etc., in doubles); every call spans all `batch` chains.
+ * Replaces FiniteDMRG.run (tnpy/finite_dmrg.py:214-257) called once per chain: the one-site
+ * matvec (:411-440 of matrix_product_state.py), dense H_eff (:372-409), environment update
+ * (:296-336), the eigensolver (linalg.eigshmv, tnpy/linalg.py:64-87) and the gauge move
+ * (:187-225), each for all chains at once. precision: TNX_FP64 native FP64 GEMMs, TNX_DF64 or
+ * TNX_BF16X3 double-FP32 GEMMs (FP64-class results from the FP32 pipe). */
+size_t tnx_batched_matvec1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                                           int batch);
+int tnx_batched_matvec1(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR,
+                        const double* x, int64_t sx, double* y, int64_t sy, int batch, int64_t chi_l, int64_t d,
+                        int64_t chi_r, int64_t dl, int64_t dr, int precision, void* workspace,
+                        size_t workspace_bytes, void* stream);
+/* H[b] (n x n, n = chi_l d chi_r <= 4096) stored at H + b n^2 */
+int tnx_batched_full_matrix1(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR,
+                             double* H, int batch, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                             void* stream);
+size_t tnx_batched_env_update_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                                              int batch);
+int tnx_batched_env_update(int direction, const double* E_in, int64_t sE, const double* A, int64_t sA,
+                           const double* W, int64_t sW, double* E_out, int64_t sO, int batch, int64_t chi_l, int64_t d,
+                           int64_t chi_r, int64_t dl, int64_t dr, int precision, void* workspace,
+                           size_t workspace_bytes, void* stream);
+/* Davidson for every chain in the same launches, with a per-chain convergence mask: chain b
+ * retires once ||H x - theta x|| <= tol max(1, |theta|) (or its correction vanishes against its
+ * basis) and every vector kernel skips it from then on. X: in = start vectors, out = unit Ritz
+ * vectors. evals_out / resid_out (device, batch doubles), active_out (device, batch ints, may
+ * be null): 1 for chains still unconverged after max_iter expansions (TNX_ERR_NOT_CONVERGED),
+ * *iters_out = expansions run. One host read (the active count) per expansion. */
+size_t tnx_batched_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                                             int batch, int max_basis);
+int tnx_batched_davidson1(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR,
+                          double* X, int64_t sX, int batch, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl,
+                          int64_t dr, double tol, int max_iter, int max_basis, int precision, double* evals_out,
+                          double* resid_out, int* iters_out, int* active_out, void* workspace,
+                          size_t workspace_bytes, void* stream);
+/* Gauge move of every chain (same contract as tnx_gauge_move): one Householder QR per chain in
+ * shared memory (site matrix m x n with m n <= 12800, n <= 128), then the neighbours take R. */
+size_t tnx_batched_gauge_move_workspace_bytes(int direction, int64_t chi_l, int64_t d, int64_t chi_r,
+                                              int64_t chi_other, int batch);
+int tnx_batched_gauge_move(int direction, double* A_site, int64_t sA, double* A_nb, int64_t sN, int batch,
+                           int64_t chi_l, int64_t d, int64_t chi_r, int64_t chi_other, int precision, void* workspace,
+                           size_t workspace_bytes, void* stream);
+
 /* ---- tSDRG ----------------------------------------------------------------------------
  * Batched two-block Hamiltonians (TreeTensorNetworkSDRG.block_hamiltonian,
  * tnpy/tsdrg.py:607-631): item b multiplies W1_b[0,w] (x) W2_b[w,dr2-1] over the MPO bond w:

@@ -77,6 +77,20 @@ SIGNATURES = {
     "tnx_tsdrg_project": (_int, [_vp, _vp, _vp, _vp, _int, _vp, _int, _int, _int, _int, _vp]),
     "tnx_tsdrg_block_eigh_workspace_bytes": (_sz, [_int, _int, _int, _int]),
     "tnx_tsdrg_block_eigh": (_int, [_vp, _vp, _vp, _int, _int, _int, _int, _int, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "tnx_batched_matvec1_workspace_bytes": (_sz, [_i64, _i64, _i64, _i64, _i64, _int]),
+    "tnx_batched_matvec1": (_int, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _int, _i64, _i64, _i64,
+                                   _i64, _i64, _int, _vp, _sz, _vp]),
+    "tnx_batched_full_matrix1": (_int, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _int, _i64, _i64, _i64, _i64, _i64,
+                                        _vp]),
+    "tnx_batched_env_update_workspace_bytes": (_sz, [_i64, _i64, _i64, _i64, _i64, _int]),
+    "tnx_batched_env_update": (_int, [_int, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _int, _i64, _i64, _i64,
+                                      _i64, _i64, _int, _vp, _sz, _vp]),
+    "tnx_batched_davidson1_workspace_bytes": (_sz, [_i64, _i64, _i64, _i64, _i64, _int, _int]),
+    "tnx_batched_davidson1": (_int, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _int, _i64, _i64, _i64, _i64,
+                                     _i64, _dbl, _int, _int, _int, _vp, _vp, _pi, _vp, _vp, _sz, _vp]),
+    "tnx_batched_gauge_move_workspace_bytes": (_sz, [_int, _i64, _i64, _i64, _i64, _int]),
+    "tnx_batched_gauge_move": (_int, [_int, _vp, _i64, _vp, _i64, _int, _i64, _i64, _i64, _i64, _int, _vp, _sz,
+                                      _vp]),
     "tnx_autotune_set": (_int, [_int]),
     "tnx_autotune_clear": (_int, []),
     "tnx_autotune_count": (_int, []),

@@ -231,8 +231,16 @@ constexpr int RR_T = 128;  // threads of the Rayleigh-Ritz kernel
 // the FP32 eigenbasis, s <- s - sum_j v_j (v_j . r) / (l_j - theta), and the FP64 Rayleigh
 // quotient. FP32 rounding keeps regenerating off-diagonal entries at ~6e-8 |A|_F, so the sweeps
 // stop once every off-diagonal entry is below 1e-6 |A|_F; the FP64 steps take it from there.
+// Batched form: block b solves the matrix at A + b sA into eval[b sE], evec + b sV, and returns at
+// once when active is given and active[b] == 0.
 __global__ void __launch_bounds__(RR_T) rr_lowest_warp_kernel(const double* __restrict__ A, int n, int ld,
-                                                            double* __restrict__ eval, double* __restrict__ evec) {
+                                                            double* __restrict__ eval, double* __restrict__ evec,
+                                                            int64_t sA, int64_t sE, int64_t sV,
+                                                            const int* __restrict__ active) {
+  if (active && !active[blockIdx.x]) return;
+  A += int64_t(blockIdx.x) * sA;
+  eval += int64_t(blockIdx.x) * sE;
+  evec += int64_t(blockIdx.x) * sV;
   extern __shared__ double sm_d[];
   double* Ad = sm_d;                                      // n x n FP64
   float* Af = reinterpret_cast<float*>(Ad + n * n);       // n x (n+1) FP32
@@ -394,10 +402,16 @@ size_t rr_lowest_smem(int n) {
 }
 
 int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cudaStream_t st) {
+  return rr_lowest_f64_batched(A, n, ld, 0, eval, 0, evec, 0, 1, nullptr, st);
+}
+
+int rr_lowest_f64_batched(const double* A, int n, int ld, int64_t sA, double* eval, int64_t sE, double* evec,
+                          int64_t sV, int batch, const int* active, cudaStream_t st) {
   if (n > RW_MAX) {
     set_error("rr_lowest_f64: n=%d > %d", n, RW_MAX);
     return TNX_ERR_SHAPE;
   }
+  if (batch <= 0) return TNX_OK;
   static std::atomic<bool> attr{false};  // idempotent setup; threads may race to it
   const size_t smem = rr_lowest_smem(RW_MAX);
   if (!attr.load()) {
@@ -405,7 +419,7 @@ int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cu
     attr.store(true);
   }
   profile_mark(KF_EIGH, st, true);
-  rr_lowest_warp_kernel<<<1, RR_T, rr_lowest_smem(n), st>>>(A, n, ld, eval, evec);
+  rr_lowest_warp_kernel<<<batch, RR_T, rr_lowest_smem(n), st>>>(A, n, ld, eval, evec, sA, sE, sV, active);
   profile_mark(KF_EIGH, st, false);
   TNX_LAUNCH_CHECK();
   return TNX_OK;

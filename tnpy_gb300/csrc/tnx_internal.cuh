@@ -230,6 +230,10 @@ int eigh_small_f64_uniform(const double* A, int n, int ld, int keep, double* eva
                            double* work, cudaStream_t st);
 // lowest eigenpair of one n x n (n <= 64) matrix, one warp: FP32 Jacobi + FP64 refinement
 int rr_lowest_f64(const double* A, int n, int ld, double* eval, double* evec, cudaStream_t st);
+// the same for `batch` matrices at A + b sA (results at eval + b sE, evec + b sV); blocks whose
+// active[b] is 0 return at once (active may be null)
+int rr_lowest_f64_batched(const double* A, int n, int ld, int64_t sA, double* eval, int64_t sE, double* evec,
+                          int64_t sV, int batch, const int* active, cudaStream_t st);
 int eigh_small_f64(double* A, const int64_t* offsets, const int* sizes, int batch, int max_size,
                    int keep, double* evals, double* evecs, double* work, cudaStream_t st);
 

@@ -287,7 +287,154 @@ class FiniteDMRG:
 
 
 class BatchedFiniteDMRG:
-    """Many independent chains (disorder realisations, parameter scans) swept concurrently.
+    """Many independent chains of one shape (disorder realisations, parameter scans) swept in
+    lockstep, every kernel spanning all chains: FiniteDMRG.run (finite_dmrg.py:214-257) per chain,
+    computed as one stacked problem.
+
+    Chain c starts from MatrixProductState.random(n, bond_dim, d, seed=seeds[c]) (default
+    seeds: ``seed + c``) exactly as ``FiniteDMRG(mpos[c], bond_dim, seed=seeds[c])`` does, and
+    each site update applies the reference's steps to every chain at once: the lowest eigenpair
+    (dense Jacobi below ``exact_solver_dim`` elements, else the batched Davidson with a per-chain
+    convergence mask), the 1e-5 perturbation, the QR gauge move and the environment update. A
+    chain stops recording energies once its |dE| < tol (its ``energies`` end there, as in
+    FiniteDMRG.run); the batch sweeps until every chain has converged or max_sweep.
+
+    ``precision``: 'fp64' native FP64 GEMMs; 'mixed' (or 'df64') double-FP32 GEMMs on the FP32
+    pipe (FP64-class products, ~2^-48 per product) for the matvecs, environment updates and
+    gauge moves; the Rayleigh-Ritz, Gram-Schmidt and residuals stay FP64."""
+
+    def __init__(self, mpos, bond_dim: int | None = None, *, chi: int | None = None, seed: int = 100,
+                 seeds=None, precision: str = "fp64", exact_solver_dim: int = 200, max_iter: int = 400,
+                 max_basis: int = 24, device=None):
+        mpos = list(mpos)
+        if not mpos:
+            raise ValueError("BatchedFiniteDMRG needs at least one MPO")
+        bond_dim = bond_dim if bond_dim is not None else chi
+        if bond_dim is None:
+            raise TypeError("BatchedFiniteDMRG needs bond_dim (or chi)")
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        n, d = mpos[0].n_sites, mpos[0].phys_dim
+        ws = [m.device_tensors(self.device) for m in mpos]
+        for m, w in zip(mpos, ws):
+            if m.n_sites != n or m.phys_dim != d or any(a.shape != b.shape for a, b in zip(w, ws[0])):
+                raise ValueError("BatchedFiniteDMRG stacks chains of one shape (n, d, MPO bonds); use "
+                                 "StreamedFiniteDMRG for mixed shapes")
+        self.n_chains, self._n, self._d = len(mpos), n, d
+        self._bond_dim = int(bond_dim)
+        self.precision = precision
+        K.precision_code(precision)
+        self._exact_solver_dim = exact_solver_dim
+        self.max_iter, self.max_basis = max_iter, max_basis
+        seeds = list(seeds) if seeds is not None else [seed + c for c in range(self.n_chains)]
+        if len(seeds) != self.n_chains:
+            raise ValueError("one seed per chain")
+        self.seeds = seeds
+        # per site: stacked [B, ...] tensors
+        self._w = [torch.stack([w[s] for w in ws]).contiguous() for s in range(n)]
+        states = [MatrixProductState.random(n, self._bond_dim, d, seed=sd, device=self.device) for sd in seeds]
+        self._t = [torch.stack([m.tensors[s] for m in states]).contiguous() for s in range(n)]
+        del states
+        B = self.n_chains
+        one = torch.ones((B, 1, 1, 1), dtype=torch.float64, device=self.device)
+        self._left = {0: one}
+        self._right = {n - 1: one.clone()}
+        for s in range(1, n):
+            self._left[s] = K.batched_env_update(1, self._left[s - 1], self._t[s - 1], self._w[s - 1],
+                                                 precision=self.precision)
+        for s in range(n - 2, -1, -1):
+            self._right[s] = K.batched_env_update(-1, self._right[s + 1], self._t[s + 1], self._w[s + 1],
+                                                  precision=self.precision)
+        self._energies: list[list[float]] = [[] for _ in range(B)]
+        self.converged = [False] * B
+        self.sweeps = [0] * B
+        self.sweep_seconds: list[float] = []
+        self.stats = {"dense_solves": 0, "iterative_solves": 0, "expansions": 0, "unconverged": 0}
+
+    @property
+    def n_sites(self) -> int:
+        return self._n
+
+    @property
+    def bond_dim(self) -> int:
+        return self._bond_dim
+
+    @property
+    def energies(self) -> list[list[float]]:
+        return [list(e) for e in self._energies]
+
+    def mps(self, chain: int) -> MatrixProductState:
+        """Chain ``chain``'s MPS (copies of its site tensors)."""
+        return MatrixProductState([t[chain].clone() for t in self._t], device=self.device)
+
+    def _solve(self, site: int, tol: float) -> torch.Tensor:
+        x = self._t[site]
+        L, W, R = self._left[site], self._w[site], self._right[site]
+        B = self.n_chains
+        if x[0].numel() < self._exact_solver_dim:
+            self.stats["dense_solves"] += 1
+            H = K.batched_full_matrix1(L, W, R)
+            evals, evecs = K.eigh_batched(list(H), keep=1)
+            self._t[site] = evecs[:, : x[0].numel(), 0].reshape(x.shape).contiguous()
+            return evals[:, 0]
+        self.stats["iterative_solves"] += 1
+        X = x.clone()
+        evals, resid, its, active = K.batched_davidson1(L, W, R, X, tol=tol, max_iter=self.max_iter,
+                                                        max_basis=self.max_basis, precision=self.precision)
+        self.stats["expansions"] += its
+        n_bad = int(active.sum().item())
+        if n_bad:
+            self.stats["unconverged"] += n_bad
+            logger.warning(f"site {site}: {n_bad} of {B} chains' Davidson did not converge after {its} expansions")
+        self._t[site] = X
+        return evals
+
+    def sweep(self, direction: Direction = Direction.RIGHTWARD, tol: float = 1e-8) -> torch.Tensor:
+        """One sweep of every chain (finite_dmrg.py:143-171); returns each chain's last local
+        energy (device tensor [B])."""
+        n = self._n
+        sites = range(n - 1) if direction == Direction.RIGHTWARD else range(n - 1, 0, -1)
+        e = None
+        for site in sites:
+            e = self._solve(site, tol)
+            psi = self._t[site]
+            hpsi = K.batched_matvec1(self._left[site], self._w[site], self._right[site], psi,
+                                     precision=self.precision)
+            psi.add_(hpsi, alpha=1e-5)
+            if direction == Direction.RIGHTWARD:
+                K.batched_gauge_move(1, self._t[site], self._t[site + 1], precision=self.precision)
+                self._left[site + 1] = K.batched_env_update(1, self._left[site], self._t[site], self._w[site],
+                                                            precision=self.precision)
+            else:
+                K.batched_gauge_move(-1, self._t[site], self._t[site - 1], precision=self.precision)
+                self._right[site - 1] = K.batched_env_update(-1, self._right[site], self._t[site], self._w[site],
+                                                             precision=self.precision)
+        return e
+
+    def run(self, tol: float = 1e-8, max_sweep: int = 100, metric: Metric = Metric.ENERGY) -> list[list[float]]:
+        """Sweep all chains until each has |dE| < tol (per chain) or ``max_sweep`` sweeps;
+        returns every chain's per-sweep energies up to its convergence."""
+        if metric != Metric.ENERGY:
+            raise NotImplementedError("batched chains converge on the energy metric")
+        for n_sweep, direction in zip(range(1, max_sweep + 1), cycle([Direction.RIGHTWARD, Direction.LEFTWARD])):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e = self.sweep(direction, tol=tol).cpu().numpy()
+            self.sweep_seconds.append(time.perf_counter() - t0)
+            for c in range(self.n_chains):
+                if self.converged[c]:
+                    continue
+                self._energies[c].append(float(e[c]))
+                self.sweeps[c] = n_sweep
+                if len(self._energies[c]) >= 2 and abs(self._energies[c][-1] - self._energies[c][-2]) < tol:
+                    self.converged[c] = True
+            if all(self.converged):
+                break
+        return self.energies
+
+
+class StreamedFiniteDMRG:
+    """Many independent chains of any shapes swept concurrently on CUDA streams (for chains that
+    BatchedFiniteDMRG cannot stack because their sizes differ).
 
     Each chain is a ``FiniteDMRG`` built and swept on its own CUDA stream by one of ``workers``
     host threads (chain c on worker c mod workers). Every library call releases the GIL and a
@@ -301,10 +448,10 @@ class BatchedFiniteDMRG:
                  device=None, **kwargs):
         self._mpos = list(mpos)
         if not self._mpos:
-            raise ValueError("BatchedFiniteDMRG needs at least one MPO")
+            raise ValueError("StreamedFiniteDMRG needs at least one MPO")
         self._bond_dim = bond_dim if bond_dim is not None else chi
         if self._bond_dim is None:
-            raise TypeError("BatchedFiniteDMRG needs bond_dim (or chi)")
+            raise TypeError("StreamedFiniteDMRG needs bond_dim (or chi)")
         self._kwargs = kwargs
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.workers = max(1, min(int(workers), len(self._mpos)))

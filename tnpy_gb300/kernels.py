@@ -265,3 +265,111 @@ def gemm_oz(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False):
     check("tnx_gemm_oz", lib.tnx_gemm_oz(int(trans_a), int(trans_b), m, n, k, 1.0, ptr(a), a.shape[1], ptr(b),
                                          b.shape[1], 0.0, ptr(out), n, wp, wn, stream_ptr()))
     return out
+
+
+# ---- chains batched in lockstep ([B, ...] stacked tensors; every call spans all chains) ----
+def _stacked(t: torch.Tensor, name: str, nd: int) -> torch.Tensor:
+    t = _f64(t, name)
+    if t.ndim != nd:
+        raise ValueError(f"{name} must be a stacked [B, ...] tensor with {nd} dimensions (got {tuple(t.shape)})")
+    return t
+
+
+def _bsite_dims(L, W, R):
+    B, chi_l, dl, chi_l2 = L.shape
+    B2, dl2, dr, d, d2 = W.shape
+    B3, chi_r, dr2, chi_r2 = R.shape
+    if len({B, B2, B3}) != 1 or chi_l != chi_l2 or chi_r != chi_r2 or dl != dl2 or dr != dr2 or d != d2:
+        raise ValueError(f"inconsistent batched L {tuple(L.shape)}, W {tuple(W.shape)}, R {tuple(R.shape)}")
+    return B, chi_l, d, chi_r, dl, dr
+
+
+def batched_matvec1(L, W, R, x, precision="fp64"):
+    """y[b] = H_eff[b] x[b] for every chain b (L [B, chi_l, dl, chi_l], W [B, dl, dr, d, d],
+    R [B, chi_r, dr, chi_r], x [B, chi_l, d, chi_r])."""
+    L, W, R, x = _stacked(L, "L", 4), _stacked(W, "W", 5), _stacked(R, "R", 4), _stacked(x, "x", 4)
+    B, chi_l, d, chi_r, dl, dr = _bsite_dims(L, W, R)
+    y = torch.empty_like(x)
+    wp, wn = Workspace.get(lib.tnx_batched_matvec1_workspace_bytes(chi_l, d, chi_r, dl, dr, B), x.device)
+    n = chi_l * d * chi_r
+    check("tnx_batched_matvec1", lib.tnx_batched_matvec1(
+        ptr(L), chi_l * dl * chi_l, ptr(W), dl * dr * d * d, ptr(R), chi_r * dr * chi_r, ptr(x), n, ptr(y), n, B,
+        chi_l, d, chi_r, dl, dr, precision_code(precision), wp, wn, stream_ptr()))
+    return y
+
+
+def batched_full_matrix1(L, W, R):
+    L, W, R = _stacked(L, "L", 4), _stacked(W, "W", 5), _stacked(R, "R", 4)
+    B, chi_l, d, chi_r, dl, dr = _bsite_dims(L, W, R)
+    n = chi_l * d * chi_r
+    H = torch.empty((B, n, n), dtype=torch.float64, device=L.device)
+    check("tnx_batched_full_matrix1", lib.tnx_batched_full_matrix1(
+        ptr(L), chi_l * dl * chi_l, ptr(W), dl * dr * d * d, ptr(R), chi_r * dr * chi_r, ptr(H), B, chi_l, d, chi_r,
+        dl, dr, stream_ptr()))
+    return H
+
+
+def batched_env_update(direction: int, E, A, W, precision="fp64"):
+    E, A, W = _stacked(E, "E", 4), _stacked(A, "A", 4), _stacked(W, "W", 5)
+    B, chi_l, d, chi_r = A.shape
+    dl, dr = W.shape[1], W.shape[2]
+    if direction == 1:
+        if tuple(E.shape) != (B, chi_l, dl, chi_l):
+            raise ValueError(f"left environments {tuple(E.shape)} do not match A {tuple(A.shape)} / W")
+        shape = (B, chi_r, dr, chi_r)
+    elif direction == -1:
+        if tuple(E.shape) != (B, chi_r, dr, chi_r):
+            raise ValueError(f"right environments {tuple(E.shape)} do not match A {tuple(A.shape)} / W")
+        shape = (B, chi_l, dl, chi_l)
+    else:
+        raise KeyError("direction must be +1 (rightward) or -1 (leftward)")
+    out = torch.empty(shape, dtype=torch.float64, device=A.device)
+    wp, wn = Workspace.get(lib.tnx_batched_env_update_workspace_bytes(chi_l, d, chi_r, dl, dr, B), A.device)
+    check("tnx_batched_env_update", lib.tnx_batched_env_update(
+        direction, ptr(E), E[0].numel(), ptr(A), A[0].numel(), ptr(W), W[0].numel(), ptr(out), out[0].numel(), B,
+        chi_l, d, chi_r, dl, dr, precision_code(precision), wp, wn, stream_ptr()))
+    return out
+
+
+def batched_davidson1(L, W, R, X, tol=1e-8, max_iter=400, max_basis=24, precision="fp64"):
+    """Lowest eigenpair of every chain's H_eff from X[b] (overwritten with the unit Ritz vectors).
+    Returns (evals [B], residuals [B], expansions, active mask [B] of chains not converged)."""
+    L, W, R = _stacked(L, "L", 4), _stacked(W, "W", 5), _stacked(R, "R", 4)
+    if X.dtype != torch.float64 or not X.is_cuda or not X.is_contiguous() or X.ndim != 4:
+        raise ValueError("X must be a contiguous float64 CUDA tensor [B, chi_l, d, chi_r] (it is overwritten)")
+    B, chi_l, d, chi_r, dl, dr = _bsite_dims(L, W, R)
+    n = chi_l * d * chi_r
+    evals = torch.empty(B, dtype=torch.float64, device=X.device)
+    resid = torch.empty(B, dtype=torch.float64, device=X.device)
+    active = torch.empty(B, dtype=torch.int32, device=X.device)
+    wp, wn = Workspace.get(lib.tnx_batched_davidson1_workspace_bytes(chi_l, d, chi_r, dl, dr, B, max_basis), X.device)
+    it = ctypes.c_int(0)
+    st = lib.tnx_batched_davidson1(ptr(L), chi_l * dl * chi_l, ptr(W), dl * dr * d * d, ptr(R), chi_r * dr * chi_r,
+                                   ptr(X), n, B, chi_l, d, chi_r, dl, dr, float(tol), int(max_iter), int(max_basis),
+                                   precision_code(precision), ptr(evals), ptr(resid), ctypes.byref(it), ptr(active),
+                                   wp, wn, stream_ptr())
+    if st not in (_lib.TNX_OK, _lib.TNX_ERR_NOT_CONVERGED):
+        check("tnx_batched_davidson1", st)
+    return evals, resid, it.value, active
+
+
+def batched_gauge_move(direction: int, a_site: torch.Tensor, a_nb: torch.Tensor, precision="fp64"):
+    """In-place gauge move of every chain (QR form of split_tensor) on stacked site tensors."""
+    if not (a_site.is_contiguous() and a_nb.is_contiguous()) or a_site.ndim != 4 or a_nb.ndim != 4:
+        raise ValueError("stacked MPS tensors [B, chi_l, d, chi_r] must be contiguous")
+    B, chi_l, d, chi_r = a_site.shape
+    if direction == 1:
+        if a_nb.shape[1] != chi_r:
+            raise ValueError("right neighbour does not share the bond")
+        other = a_nb.shape[3]
+    elif direction == -1:
+        if a_nb.shape[3] != chi_l:
+            raise ValueError("left neighbour does not share the bond")
+        other = a_nb.shape[1]
+    else:
+        raise KeyError("MatrixProductState only supplies left or right direction.")
+    wp, wn = Workspace.get(lib.tnx_batched_gauge_move_workspace_bytes(direction, chi_l, d, chi_r, other, B),
+                           a_site.device)
+    check("tnx_batched_gauge_move", lib.tnx_batched_gauge_move(
+        direction, ptr(a_site), a_site[0].numel(), ptr(a_nb), a_nb[0].numel(), B, chi_l, d, chi_r, other,
+        precision_code(precision), wp, wn, stream_ptr()))

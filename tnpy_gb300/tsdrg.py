@@ -422,9 +422,12 @@ class TreeTensorNetworkSDRG:
 
     @property
     def measurements(self):
+        """TreeTensorNetworkMeasurements of the finished tree (tsdrg.py:698-708)."""
         if not self._chain.done:
             raise RuntimeError("tSDRG algorithm hasn't been executed yet.")
-        raise NotImplementedError("tree measurements are not part of this build")
+        from .tsdrg_measurements import TreeTensorNetworkMeasurements
+
+        return TreeTensorNetworkMeasurements(self._chain.tree, phys_dim=self._mpo.phys_dim, device=self._dev)
 
 
 TSDRG = TreeTensorNetworkSDRG
