@@ -263,6 +263,19 @@ int tnx_tsdrg_block_eigh(const double* const* w1, const double* const* w2, const
                          double* evecs, int* iters, void* workspace, size_t workspace_bytes,
                          void* stream);
 
+/* ---- exact diagonalisation --------------------------------------------------------------
+ * Dense Hamiltonian of an MPO (FullHamiltonian, tnpy/operators.py:119-166): W is the MPO packed
+ * as [n][D][D][d][d] (the uniform four-index tensors padded with zeros to bond D <= 32: site 0
+ * uses row 0, site n-1 column 0); H (d^n x d^n, row-major, d^n <= 65536) gets
+ * H[K][B] = e_0^T W_0[:,:,k_0,b_0] ... W_{n-1}[:,:,k_{n-1},b_{n-1}] e_0, with k_0 / b_0 the most
+ * significant digits of the ket / bra strings K / B. */
+int tnx_full_hamiltonian(const double* W, int n, int D, int d, double* H, void* stream);
+/* H += c I with c = max_i sum_j |H_ij| + 1 written to *shift (device double), which makes a
+ * symmetric H positive definite; undo = 1 subtracts the c already in *shift. With tnx_svd this
+ * gives the full spectrum of ExactDiagonalization (tnpy/exact_diagonalization.py:10-60):
+ * eigenvalues = singular values - c, eigenvectors = left singular vectors. */
+int tnx_shift_to_spd(double* H, int64_t dim, double* shift, int undo, void* stream);
+
 /* ---- generic helpers used by the host mirror ------------------------------------------ */
 /* C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b], row-major, FP64; trans_a / trans_b = 1
  * means A is stored K x M / B is stored N x K. */

@@ -42,7 +42,8 @@ def right_canonicalize(mps: list[np.ndarray]) -> list[np.ndarray]:
         k = q.shape[1]
         mps[i] = q.T.reshape(k, d, cr)
         mps[i - 1] = np.tensordot(mps[i - 1], r.T, axes=([2], [0]))
-    mps[0] = mps[0] / np.linalg.norm(mps[0])
+        # unit norm at every step (a product of ~n random tensors overflows on long chains)
+        mps[i - 1] = mps[i - 1] / np.linalg.norm(mps[i - 1])
     return mps
 
 

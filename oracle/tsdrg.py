@@ -50,6 +50,12 @@ def spectrum_projector(w1: np.ndarray, w2: np.ndarray, evecs: np.ndarray):
 
 
 class TreeTensorNetworkSDRG:
+    def solve(self, h: np.ndarray):
+        return block_eigen_solver(h, self.chi)
+
+    def gap_of(self, evals: np.ndarray) -> float:
+        return truncation_gap(evals, self.chi)
+
     def __init__(self, mpo, chi: int):
         self.chi = chi
         self.n = len(mpo)
@@ -61,9 +67,9 @@ class TreeTensorNetworkSDRG:
         self.gap: list[float] = []
         self.evecs: list[np.ndarray] = []
         for bond in range(self.n - 1):
-            ev, vec = block_eigen_solver(block_hamiltonian(self.cache[bond], self.cache[bond + 1]), chi)
+            ev, vec = self.solve(block_hamiltonian(self.cache[bond], self.cache[bond + 1]))
             self.evecs.append(vec)
-            self.gap.append(truncation_gap(ev, chi))
+            self.gap.append(self.gap_of(ev))
             self.evals = ev if self.n == 2 else None
 
     def _neighbours(self, bond: int):
@@ -93,10 +99,42 @@ class TreeTensorNetworkSDRG:
             self.gap.pop(b)
             self.evecs.pop(b)
             for bond in self._neighbours(b):
-                ev, vec = block_eigen_solver(
-                    block_hamiltonian(self.cache[bond], self.cache[bond + 1]), self.chi
-                )
-                self.gap[bond] = truncation_gap(ev, self.chi)
+                ev, vec = self.solve(block_hamiltonian(self.cache[bond], self.cache[bond + 1]))
+                self.gap[bond] = self.gap_of(ev)
                 self.evecs[bond] = vec
                 self.evals = ev
         return self
+
+
+class HighEnergyTreeTensorNetworkSDRG(TreeTensorNetworkSDRG):
+    """tsdrg.py:1031-1067: keep the chi highest pairs; gap evals[-chi] - evals[-chi-1], or the
+    first gap of a spectrum with at most chi gaps."""
+
+    def solve(self, h: np.ndarray):
+        evals, evecs = np.linalg.eigh(h)
+        if h.shape[0] > self.chi:
+            evals, evecs = evals[-self.chi:], evecs[:, -self.chi:]
+        return evals, evecs
+
+    def gap_of(self, evals: np.ndarray) -> float:
+        gaps = np.diff(evals)
+        return float(gaps[-self.chi] if gaps.size > self.chi else gaps[0])
+
+
+class ShiftInvertTreeTensorNetworkSDRG(TreeTensorNetworkSDRG):
+    """tsdrg.py:1070-1089: generalised eigh(H, H^2) (eigenvalues 1/E), keep the chi smallest,
+    report 1/lambda + offset in ascending order with the vectors H x (unit norm)."""
+
+    def __init__(self, mpo, chi: int, offset: float):
+        self.offset = offset
+        super().__init__(mpo, chi)
+
+    def solve(self, h: np.ndarray):
+        import scipy.linalg as spl
+
+        evals, evecs = spl.eigh(h, b=h @ h)
+        if h.shape[0] > self.chi:
+            evals, evecs = evals[: self.chi], evecs[:, : self.chi]
+        evals = np.reciprocal(evals) + self.offset
+        idx = np.argsort(evals)
+        return evals[idx], h @ evecs[:, idx]

@@ -165,3 +165,30 @@ def test_batched_n128_chi32_kept_spectra_vs_one_at_a_time_fp64(cuda, seed):
     o = ots.TreeTensorNetworkSDRG(_oracle_chain(n, seed, 0.5), chi).run()
     np.testing.assert_allclose(b.evals[0], o.evals, atol=1e-10)
     assert [list(m) for m in b.merges[0]] == [list(m) for m in o.merges]
+
+
+@pytest.mark.parametrize("variant", ["high_energy", "shift_invert"])
+def test_tsdrg_variants_vs_oracle(cuda, variant):
+    """HighEnergyTreeTensorNetworkSDRG (tnpy/tsdrg.py:1031-1067) and
+    ShiftInvertTreeTensorNetworkSDRG (:1070-1089) against their restatements: kept spectra of
+    the last block and the merge order."""
+    import tnpy_gb300 as tg
+
+    n, chi = 10, 8
+    arr = om.random_heisenberg_mpo(n, 0.5, seed=4)
+    mpo = tg.MatrixProductOperator(arr)
+    if variant == "high_energy":
+        t = tg.HighEnergyTreeTensorNetworkSDRG(mpo, chi=chi)
+        o = ots.HighEnergyTreeTensorNetworkSDRG(arr, chi)
+    else:
+        t = tg.ShiftInvertTreeTensorNetworkSDRG(mpo, chi=chi, offset=0.0)
+        o = ots.ShiftInvertTreeTensorNetworkSDRG(arr, chi, 0.0)
+    t.run()
+    o.run()
+    np.testing.assert_allclose(t.evals, o.evals, atol=1e-10)
+    assert [[n_.left.node_id, n_.right.node_id, n_.node_id] for n_ in t.tree if not n_.is_leaf] == \
+        [list(m) for m in o.merges]
+    if variant == "high_energy":
+        # the kept states are the highest of the chain: <H> of the root states through the tree
+        ev = np.sort(t.measurements.expectation_value(mpo))
+        np.testing.assert_allclose(ev, np.sort(o.evals), atol=1e-10)

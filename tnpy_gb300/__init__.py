@@ -22,11 +22,20 @@ from .matrix_product_state import (  # noqa: E402
     MatrixProductState,
     MatrixProductStateMeasurements,
 )
+from .exact_diagonalization import ExactDiagonalization  # noqa: E402
 from .operators import FullHamiltonian, MatrixProductOperator, SpinOperators  # noqa: E402
-from .tsdrg import TSDRG, BatchedTSDRG, TensorTree, TreeTensorNetworkSDRG  # noqa: E402
+from .tsdrg import (  # noqa: E402
+    TSDRG,
+    BatchedTSDRG,
+    HighEnergyTreeTensorNetworkSDRG,
+    ShiftInvertTreeTensorNetworkSDRG,
+    TensorTree,
+    TreeTensorNetworkSDRG,
+)
 
 __all__ = [
     "FiniteDMRG", "BatchedFiniteDMRG", "StreamedFiniteDMRG", "Metric", "Direction", "Environment", "MatrixProductState",
     "MatrixProductStateMeasurements", "FullHamiltonian", "MatrixProductOperator", "SpinOperators",
-    "linalg", "model", "logger", "TSDRG", "TreeTensorNetworkSDRG", "BatchedTSDRG", "TensorTree",
+    "linalg", "model", "logger", "ExactDiagonalization", "TSDRG", "TreeTensorNetworkSDRG", "BatchedTSDRG", "TensorTree",
+    "HighEnergyTreeTensorNetworkSDRG", "ShiftInvertTreeTensorNetworkSDRG",
 ]

@@ -91,6 +91,8 @@ SIGNATURES = {
     "tnx_batched_gauge_move_workspace_bytes": (_sz, [_int, _i64, _i64, _i64, _i64, _int]),
     "tnx_batched_gauge_move": (_int, [_int, _vp, _i64, _vp, _i64, _int, _i64, _i64, _i64, _i64, _int, _vp, _sz,
                                       _vp]),
+    "tnx_full_hamiltonian": (_int, [_vp, _int, _int, _int, _vp, _vp]),
+    "tnx_shift_to_spd": (_int, [_vp, _i64, _vp, _int, _vp]),
     "tnx_autotune_set": (_int, [_int]),
     "tnx_autotune_clear": (_int, []),
     "tnx_autotune_count": (_int, []),

@@ -121,14 +121,17 @@ class MatrixProductState:
         return mps
 
     def right_canonicalize(self):
+        """Right-canonical form with a normalised centre on site 0. The pushed factor is
+        rescaled to unit norm at every step: the norm of a product of ~n random tensors would
+        otherwise overflow FP64 on long chains (n = 200 at chi = 512)."""
         for site in range(self.n_sites - 1, 0, -1):
             K.gauge_move(-1, self._t[site], self._t[site - 1])
-        self._t[0] /= torch.linalg.vector_norm(self._t[0])
+            self._t[site - 1] /= torch.linalg.vector_norm(self._t[site - 1])
 
     def left_canonicalize(self):
         for site in range(self.n_sites - 1):
             K.gauge_move(1, self._t[site], self._t[site + 1])
-        self._t[-1] /= torch.linalg.vector_norm(self._t[-1])
+            self._t[site + 1] /= torch.linalg.vector_norm(self._t[site + 1])
 
     def save(self, filename: str):
         """Reference-shaped tensors in site order to ``.npz`` (matrix_product_state.py:118-142;

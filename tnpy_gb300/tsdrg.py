@@ -260,10 +260,13 @@ def project(pairs_v, dev) -> list[torch.Tensor]:
 class _Chain:
     """State of one realisation: coarse-grained MPO cache, horizon, gaps, kept vectors."""
 
-    def __init__(self, mpo: MatrixProductOperator, chi: int, dev, precision: str = "fp64"):
+    def __init__(self, mpo: MatrixProductOperator, chi: int, dev, precision: str = "fp64", mode: str = "lowest",
+                 offset: float = 0.0):
         self.n = mpo.n_sites
         self.chi = chi
         self.precision = precision
+        self.mode = mode  # which block eigenpairs are kept: lowest, highest, shift_invert
+        self.offset = offset
         self.cache = [w.contiguous() for w in mpo.device_tensors(dev)]
         self.tree = TensorTree(self.n)
         self.gap: list[float] = []
@@ -273,23 +276,51 @@ class _Chain:
         self.done = False
 
 
-def _gap(evals: np.ndarray, chi: int) -> float:
-    """truncation_gap (tsdrg.py:594-605), applied to the already truncated spectrum."""
+def _gap(evals: np.ndarray, chi: int, mode: str = "lowest") -> float:
+    """truncation_gap (tsdrg.py:594-605), applied to the already truncated spectrum; the
+    high-energy variant's gap (tsdrg.py:1054-1067) for mode 'highest'."""
     gaps = np.diff(evals)
+    if mode == "highest":
+        return float(gaps[-chi] if gaps.size > chi else gaps[0])
     return float(gaps[chi - 1] if gaps.size > chi else gaps[-1])
 
 
+def _select(c: "_Chain", ev: np.ndarray, vec: torch.Tensor):
+    """Kept pairs of a fully solved block for the variants: the chi highest (tsdrg.py:1044-1052),
+    or shift-invert (tsdrg.py:1078-1089): eigh(H, H^2) has eigenvalues 1/E with unit vectors
+    H x = sign(E) v, so the chi pairs of smallest 1/E are kept and reported as E + offset,
+    ascending."""
+    m = ev.size
+    if c.mode == "highest":
+        k = min(m, c.chi)
+        return ev[m - k:].copy(), vec[:, m - k:].contiguous()
+    with np.errstate(divide="ignore"):
+        lam = np.reciprocal(ev)
+    order = np.argsort(lam, kind="stable")[: min(m, c.chi)]
+    e_k = ev[order] + c.offset
+    idx = np.argsort(e_k, kind="stable")
+    sel = order[idx]
+    sign = torch.from_numpy(np.sign(ev[sel])).to(vec.device)
+    return e_k[idx].copy(), (vec[:, torch.from_numpy(sel).to(vec.device)] * sign[None, :]).contiguous()
+
+
 def _dense(idx, chains_bonds, out, dev):
-    """Dense FP64 Jacobi solve of the listed blocks (block_hamiltonian + eigh, tsdrg.py:569-631)."""
+    """Dense FP64 Jacobi solve of the listed blocks (block_hamiltonian + eigh, tsdrg.py:569-631);
+    the variants' blocks are solved in full and their kept pairs selected by _select."""
     pairs = [(chains_bonds[i][0].cache[chains_bonds[i][1]], chains_bonds[i][0].cache[chains_bonds[i][1] + 1])
              for i in idx]
     mats, sizes = block_hamiltonians(pairs, dev)
+    full = any(chains_bonds[i][0].mode != "lowest" for i in idx)
     chi = max(chains_bonds[i][0].chi for i in idx)
-    keep = min(chi, max(sizes))
+    keep = max(sizes) if full else min(chi, max(sizes))
     evals, evecs = K.eigh_batched(mats, keep=keep)
     ev_h = evals.cpu().numpy()
     for j, (i, m) in enumerate(zip(idx, sizes)):
-        kept = min(m, chains_bonds[i][0].chi)
+        c = chains_bonds[i][0]
+        if c.mode != "lowest":  # the variants: every pair of the block, then their selection
+            out[i] = _select(c, ev_h[j, :m].copy(), evecs[j, :m, :m])
+            continue
+        kept = min(m, c.chi)
         out[i] = (ev_h[j, :kept].copy(), evecs[j, :m, :kept].contiguous())
 
 
@@ -304,8 +335,8 @@ def _solve(chains_bonds, dev):
     for i, (c, b) in enumerate(chains_bonds):
         w1, w2 = c.cache[b], c.cache[b + 1]
         m = w1.shape[2] * w2.shape[2]
-        if (m > 64 and w1.shape[2] <= KRON_MAX_NODE and w2.shape[2] <= KRON_MAX_NODE and c.chi <= 32
-                and w1.shape[1] <= 6):
+        if (c.mode == "lowest" and m > 64 and w1.shape[2] <= KRON_MAX_NODE and w2.shape[2] <= KRON_MAX_NODE
+                and c.chi <= 32 and w1.shape[1] <= 6):
             kron.append(i)
         else:
             dense.append(i)
@@ -345,7 +376,7 @@ def run_chains(chains: List[_Chain], dev):
             ev, vec = res[i]
             i += 1
             c.evecs.append(vec)
-            c.gap.append(_gap(ev, c.chi))
+            c.gap.append(_gap(ev, c.chi, c.mode))
             c.evals = ev if c.n == 2 else None
     while True:
         active = [c for c in chains if not c.done]
@@ -376,7 +407,7 @@ def run_chains(chains: List[_Chain], dev):
         if resolve:
             res = _solve(resolve, dev)
             for (c, bond), (ev, vec) in zip(resolve, res):
-                c.gap[bond] = _gap(ev, c.chi)
+                c.gap[bond] = _gap(ev, c.chi, c.mode)
                 c.evecs[bond] = vec
                 c.evals = ev
     return chains
@@ -431,6 +462,30 @@ class TreeTensorNetworkSDRG:
 
 
 TSDRG = TreeTensorNetworkSDRG
+
+
+class HighEnergyTreeTensorNetworkSDRG(TreeTensorNetworkSDRG):
+    """tSDRG keeping the chi highest pairs of every block (tsdrg.py:1031-1067): blocks are
+    solved in full by the batched dense Jacobi kernel; the gap is the high-energy one."""
+
+    def __init__(self, mpo: MatrixProductOperator, chi: int, device=None):
+        super().__init__(mpo, chi, device=device)
+        self._chain = _Chain(mpo, self._chi, self._dev, "fp64", mode="highest")
+
+
+class ShiftInvertTreeTensorNetworkSDRG(TreeTensorNetworkSDRG):
+    """Shift-invert tSDRG (tsdrg.py:1070-1089) for the MPO of H - offset: each block keeps the
+    chi pairs of smallest 1/E (the states just below the offset first), reported as E + offset
+    in ascending order, with the vectors H x of the generalised problem (unit norm, sign(E) v)."""
+
+    def __init__(self, mpo: MatrixProductOperator, chi: int, offset: float, device=None):
+        super().__init__(mpo, chi, device=device)
+        self._offset = float(offset)
+        self._chain = _Chain(mpo, self._chi, self._dev, "fp64", mode="shift_invert", offset=self._offset)
+
+    @property
+    def offset(self) -> float:
+        return self._offset
 
 
 class BatchedTSDRG:
