@@ -138,6 +138,29 @@ int tnx_davidson1(const double* L, const double* W, const double* R, double* x, 
                   int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter,
                   int max_basis, int precision, double* eval_out, double* resid_out,
                   int* iters_out, void* workspace, size_t workspace_bytes, void* stream);
+/* Generalised problem A x = lambda B x, lowest lambda, for shift-invert DMRG
+ * (ShiftInvertDMRG.one_site_solver -> primme.eigsh(A, M=B), tnpy/finite_dmrg.py:345-363): A is
+ * the one-site H_eff of (L, W, R), B that of (L2, W2, R2) (environments of the MPO square,
+ * bond dl2 / dr2), B positive definite. Davidson with a B-orthonormal basis (two classical
+ * B-orthogonalisation passes, one B and one A product per expansion), correction
+ * (diag A - lambda diag B)^-1 r; stops when ||A x - lambda B x|| <= tol max(1, |lambda|), or when
+ * the residual has stagnated for 40 expansions below 1e-6 max(1, |lambda|) (the Ritz value is
+ * then accurate to ~residual^2 / gap). x: in = start vector, out = Ritz vector with x^T B x = 1.
+ * *iters_out = expansions. precision: TNX_FP64 native, TNX_DF64 / TNX_BF16X3 FP64-class products. */
+size_t tnx_gdavidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                                      int64_t dl2, int64_t dr2, int max_basis);
+int tnx_gdavidson1(const double* L, const double* W, const double* R, const double* L2, const double* W2,
+                   const double* R2, double* x, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                   int64_t dl2, int64_t dr2, double tol, int max_iter, int max_basis, int precision,
+                   double* eval_out, double* resid_out, int* iters_out, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
+/* One MPO tensor applied to one MPS tensor, out[(a,w)][k][(c,v)] = sum_b W[w][v][k][b] A[a][b][c]
+ * (out: chi_l*dl x d x chi_r*dr): the site tensors of O|psi>, as ShiftInvertDMRG restores
+ * psi = (H - eps) phi (tnpy/finite_dmrg.py:314-343). */
+int tnx_mpo_apply_site(const double* A, const double* W, double* out, int64_t chi_l, int64_t d, int64_t chi_r,
+                       int64_t dl, int64_t dr, void* stream);
+
 /* Counters of the calling host thread's last tnx_davidson1 call: out[0] matvecs of the first
  * phase, out[1] matvecs of the anchored phase (TNX_BF16X3; 0 otherwise), out[2] FP64-class
  * anchor products, out[3] thick restarts. */
@@ -214,7 +237,9 @@ int tnx_batched_env_update(int direction, const double* E_in, int64_t sE, const 
  * basis) and every vector kernel skips it from then on. X: in = start vectors, out = unit Ritz
  * vectors. evals_out / resid_out (device, batch doubles), active_out (device, batch ints, may
  * be null): 1 for chains still unconverged after max_iter expansions (TNX_ERR_NOT_CONVERGED),
- * *iters_out = expansions run. One host read (the active count) per expansion. */
+ * *iters_out = expansions run. One host read (the active count) every fourth expansion; restarts
+ * keep two vectors per chain (the Ritz vector and the previous one, GD+1), and the products of
+ * retired chains are skipped. */
 size_t tnx_batched_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
                                              int batch, int max_basis);
 int tnx_batched_davidson1(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR,

@@ -15,7 +15,7 @@ logger.setLevel(logging.WARNING)
 
 from . import _lib  # noqa: E402  (fails loudly when libtnx.so is missing)
 from . import autotune, linalg, model  # noqa: E402
-from .finite_dmrg import BatchedFiniteDMRG, FiniteDMRG, Metric, StreamedFiniteDMRG  # noqa: E402
+from .finite_dmrg import BatchedFiniteDMRG, FiniteDMRG, Metric, ShiftInvertDMRG, StreamedFiniteDMRG  # noqa: E402
 from .matrix_product_state import (  # noqa: E402
     Direction,
     Environment,
@@ -34,7 +34,7 @@ from .tsdrg import (  # noqa: E402
 )
 
 __all__ = [
-    "FiniteDMRG", "BatchedFiniteDMRG", "StreamedFiniteDMRG", "Metric", "Direction", "Environment", "MatrixProductState",
+    "FiniteDMRG", "ShiftInvertDMRG", "BatchedFiniteDMRG", "StreamedFiniteDMRG", "Metric", "Direction", "Environment", "MatrixProductState",
     "MatrixProductStateMeasurements", "FullHamiltonian", "MatrixProductOperator", "SpinOperators",
     "linalg", "model", "logger", "ExactDiagonalization", "TSDRG", "TreeTensorNetworkSDRG", "BatchedTSDRG", "TensorTree",
     "HighEnergyTreeTensorNetworkSDRG", "ShiftInvertTreeTensorNetworkSDRG",

@@ -37,9 +37,10 @@ inline unsigned bgrid(int64_t total, int threads, int64_t cap) {
 // ---- batched MPO contraction (blockIdx.y = chain) ---------------------------------------
 __global__ void bw_left_kernel(const double* __restrict__ T1, int64_t sT1, const double* __restrict__ W, int64_t sW,
                                double* __restrict__ T2, int64_t sT2, int64_t chi_l, int d, int64_t chi_r, int dl,
-                               int dr) {
+                               int dr, const int* __restrict__ mask = nullptr) {
   extern __shared__ double ws[];
   const int b = blockIdx.y;
+  if (mask && !mask[b]) return;
   T1 += b * sT1;
   W += b * sW;
   T2 += b * sT2;
@@ -279,14 +280,84 @@ __global__ void bcheck_kernel(const double* __restrict__ theta, const double* __
   if (threadIdx.x == 0) count[0] = cnt;
 }
 
-// restart to the Ritz vector: H_b = [[theta_b]], s_b = [1] (V_b[0] / AV_b[0] copied separately)
-__global__ void brestart_kernel(double* __restrict__ Hm, int64_t sH, const double* __restrict__ theta,
-                                double* __restrict__ evecs, int64_t sE, int B, const int* __restrict__ active) {
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
-    if (!active[b]) continue;
-    Hm[b * sH] = theta[b];
-    evecs[b * sE] = 1.0;
+// GD+1 restart of every active chain (one CTA per chain), to the Ritz vector x = V s and the
+// previous step's Ritz vector orthogonalised against it, s' = [s_prev; 0] - (s . s_prev) s (V is
+// orthonormal, so on the coefficients). When s_prev lies along s, the basis vector least aligned
+// with x takes its place, s' = e_j - s_j s, so every chain restarts to two vectors. Writes
+// xp = V s', axp = AV s' and the off-diagonal / second diagonal entry of the 2 x 2 projected
+// matrix [s s']^T H_k [s s'] into Hm (the caller sets Hm[0][0] = theta).
+__global__ void __launch_bounds__(BT) brestart_plus_kernel(const double* __restrict__ V, const double* __restrict__ AV,
+                                                          int64_t sV, int64_t n, int k, double* __restrict__ Hm,
+                                                          int64_t sH, int mb, const double* __restrict__ evecs,
+                                                          const double* __restrict__ evecs_prev, int64_t sE,
+                                                          double* __restrict__ xp, double* __restrict__ axp,
+                                                          int64_t sX, const int* __restrict__ active) {
+  __shared__ double s[BMB], sp[BMB];
+  __shared__ double h01, h11;
+  const int b = blockIdx.x;
+  if (!active[b]) return;
+  if (threadIdx.x == 0) {
+    const double* sc = evecs + b * sE;
+    const double* so = evecs_prev + b * sE;
+    double dot = 0.0;
+    for (int j = 0; j < k; ++j) s[j] = sc[j];
+    for (int j = 0; j < k - 1; ++j) dot += s[j] * so[j];
+    double nrm = 0.0;
+    for (int j = 0; j < k; ++j) {
+      sp[j] = (j < k - 1 ? so[j] : 0.0) - dot * s[j];
+      nrm += sp[j] * sp[j];
+    }
+    if (!(nrm > 1e-12)) {
+      int jm = 0;
+      for (int j = 1; j < k; ++j)
+        if (fabs(s[j]) < fabs(s[jm])) jm = j;
+      nrm = 0.0;
+      for (int j = 0; j < k; ++j) {
+        sp[j] = (j == jm ? 1.0 : 0.0) - s[jm] * s[j];
+        nrm += sp[j] * sp[j];
+      }
+    }
+    nrm = sqrt(nrm);
+    for (int j = 0; j < k; ++j) sp[j] /= nrm;
+    const double* H = Hm + b * sH;
+    double a01 = 0.0, a11 = 0.0;
+    for (int i = 0; i < k; ++i) {
+      double hsp = 0.0;
+      for (int j = 0; j < k; ++j) hsp += H[int64_t(i) * mb + j] * sp[j];
+      a01 += s[i] * hsp;
+      a11 += sp[i] * hsp;
+    }
+    h01 = a01;
+    h11 = a11;
   }
+  __syncthreads();
+  const double* vb = V + b * sV;
+  const double* ab = AV + b * sV;
+  double* xb = xp + b * sX;
+  double* axb = axp + b * sX;
+  for (int64_t i = threadIdx.x; i < n; i += BT) {
+    double xv = 0.0, av = 0.0;
+    for (int j = 0; j < k; ++j) {
+      xv = fma(sp[j], vb[int64_t(j) * n + i], xv);
+      av = fma(sp[j], ab[int64_t(j) * n + i], av);
+    }
+    xb[i] = xv;
+    axb[i] = av;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* H = Hm + b * sH;
+    H[1] = h01;
+    H[mb] = h01;
+    H[mb + 1] = h11;
+  }
+}
+
+// Hm_b[0][0] = theta_b for active chains
+__global__ void bset_theta_kernel(double* __restrict__ Hm, int64_t sH, const double* __restrict__ theta, int B,
+                                  const int* __restrict__ active) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x)
+    if (active[b]) Hm[b * sH] = theta[b];
 }
 
 __global__ void bsqrt_kernel(const double* __restrict__ in, double* __restrict__ out, int B) {
@@ -393,20 +464,21 @@ struct BDims {
   int64_t ne() const { return matvec1_scratch_elems(chi_l, d, chi_r, dl, dr); }
 };
 
+// mask (device, B ints, may be null): chains whose entry is 0 are skipped by every launch
 int bmatvec(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR, const double* x,
             int64_t sx, double* y, int64_t sy, int B, const BDims& g, double* T1, double* T2, bool df,
-            cudaStream_t st) {
+            cudaStream_t st, const int* mask = nullptr) {
   const int64_t ne = g.ne();
   // T1[(w,a'),(s,c)] = sum_a L[a,(w,a')] x[a,(s,c)]
   TNX_TRY(gemm_fp64_class(df, true, false, g.dl * g.chi_l, g.d * g.chi_r, g.chi_l, 1.0, L, g.dl * g.chi_l, sL, x,
-                          g.d * g.chi_r, sx, 0.0, T1, g.d * g.chi_r, ne, B, st));
+                          g.d * g.chi_r, sx, 0.0, T1, g.d * g.chi_r, ne, B, st, 0, mask));
   const size_t smem = size_t(g.dl * g.dr * g.d * g.d) * sizeof(double);
   bw_left_kernel<<<dim3(bgrid(g.chi_l * g.chi_r, 128, 64), B), 128, smem, st>>>(
-      T1, ne, W, sW, T2, ne, g.chi_l, int(g.d), g.chi_r, int(g.dl), int(g.dr));
+      T1, ne, W, sW, T2, ne, g.chi_l, int(g.d), g.chi_r, int(g.dl), int(g.dr), mask);
   TNX_LAUNCH_CHECK();
   // y[(a',s'),c'] = sum_{(c,v)} T2[(a',s'),(c,v)] R[(c,v),c']
   TNX_TRY(gemm_fp64_class(df, false, false, g.chi_l * g.d, g.chi_r, g.chi_r * g.dr, 1.0, T2, g.chi_r * g.dr, ne, R,
-                          g.chi_r, sR, 0.0, y, g.chi_r, sy, B, st));
+                          g.chi_r, sR, 0.0, y, g.chi_r, sy, B, st, 0, mask));
   return TNX_OK;
 }
 
@@ -420,7 +492,8 @@ int check_bdims(const void* a, const void* b, const void* c, const void* x, int 
 }
 
 struct BDavWs {
-  double *V, *AV, *x, *ax, *t, *diag, *Hm, *evals, *evecs, *h, *nrm2, *nrm2_0, *rn2, *T1, *T2;
+  double *V, *AV, *x, *ax, *t, *diag, *Hm, *evals, *evecs, *evecs_prev, *h, *nrm2, *nrm2_0, *rn2, *T1, *T2, *xp,
+      *axp;
   int *active, *count;
 };
 
@@ -436,7 +509,8 @@ size_t bdav_layout(const BDims& g, int B, int mb, void* base, BDavWs* w) {
   size_t oV = take(Bz * mb * n * 8), oAV = take(Bz * mb * n * 8), ox = take(Bz * n * 8), oax = take(Bz * n * 8),
          ot = take(Bz * n * 8), od = take(Bz * n * 8), oH = take(Bz * mb * mb * 8), oev = take(Bz * 8),
          oevec = take(Bz * mb * 8), oh = take(Bz * mb * 8), on = take(Bz * 8), on0 = take(Bz * 8), orn = take(Bz * 8),
-         oT1 = take(Bz * ne * 8), oT2 = take(Bz * ne * 8), oa = take(Bz * 4), oc = take(16);
+         oT1 = take(Bz * ne * 8), oT2 = take(Bz * ne * 8), oa = take(Bz * 4), oc = take(16),
+         oep = take(Bz * mb * 8), oxp = take(Bz * n * 8), oaxp = take(Bz * n * 8);
   if (w && base) {
     char* p = static_cast<char*>(base);
     w->V = reinterpret_cast<double*>(p + oV);
@@ -456,6 +530,9 @@ size_t bdav_layout(const BDims& g, int B, int mb, void* base, BDavWs* w) {
     w->T2 = reinterpret_cast<double*>(p + oT2);
     w->active = reinterpret_cast<int*>(p + oa);
     w->count = reinterpret_cast<int*>(p + oc);
+    w->evecs_prev = reinterpret_cast<double*>(p + oep);
+    w->xp = reinterpret_cast<double*>(p + oxp);
+    w->axp = reinterpret_cast<double*>(p + oaxp);
   }
   return off;
 }
@@ -606,30 +683,44 @@ int tnx_batched_davidson1(const double* L, int64_t sL, const double* W, int64_t 
     bscale_kernel<<<dim3(vchunks, B), BT, 0, st>>>(vk, sVB, n, w.nrm2, w.nrm2_0, w.active);
     TNX_LAUNCH_CHECK();
     double* avk = w.AV + int64_t(k) * n;
-    TNX_TRY(bmatvec(L, sL, W, sW, R, sR, vk, sVB, avk, sVB, B, g, w.T1, w.T2, df, st));
+    // converged chains are masked out of the products too
+    TNX_TRY(bmatvec(L, sL, W, sW, R, sR, vk, sVB, avk, sVB, B, g, w.T1, w.T2, df, st, w.active));
     // column k of the projected matrix (and its mirror row)
     bdots_kernel<<<dim3(k + 1, B), BT, 0, st>>>(w.V, sVB, n, avk, sVB, w.Hm + k, int64_t(mb) * mb, mb,
                                                 w.Hm + int64_t(k) * mb, 1, w.active);
     TNX_LAUNCH_CHECK();
     ++k;
     ++iters;
+    // the previous step's Ritz coefficients, for the GD+1 restart
+    TNX_CUDA(cudaMemcpyAsync(w.evecs_prev, w.evecs, size_t(B) * mb * 8, cudaMemcpyDeviceToDevice, st));
     TNX_TRY(rr_lowest_f64_batched(w.Hm, k, mb, int64_t(mb) * mb, w.evals, 1, w.evecs, mb, B, w.active, st));
     britz_kernel<<<B, BT, 0, st>>>(w.V, w.AV, sVB, n, k, w.evecs, mb, w.evals, w.diag, n, w.x, w.ax, w.t, n, w.rn2,
                                    w.active);
     TNX_LAUNCH_CHECK();
     bcheck_kernel<<<1, 256, 0, st>>>(w.evals, w.rn2, tol, B, w.active, w.count);
     TNX_LAUNCH_CHECK();
-    TNX_CUDA(cudaMemcpyAsync(&host_count, w.count, sizeof(int), cudaMemcpyDeviceToHost, st));
-    TNX_CUDA(cudaStreamSynchronize(st));
-    if (host_count == 0 || iters >= max_iter || k >= n) break;
-    if (k == mb) {  // thick restart of every active chain to its Ritz vector
+    // the active count is read every 4th expansion (the kernels already skip retired chains, so
+    // the expansions in between cost only launches once every chain has converged)
+    if (iters % 4 == 0 || iters >= max_iter || k >= n) {
+      TNX_CUDA(cudaMemcpyAsync(&host_count, w.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+      TNX_CUDA(cudaStreamSynchronize(st));
+      if (host_count == 0 || iters >= max_iter || k >= n) break;
+    }
+    if (k == mb) {  // GD+1 restart of every active chain: its Ritz vector and the previous one
+      brestart_plus_kernel<<<B, BT, 0, st>>>(w.V, w.AV, sVB, n, k, w.Hm, int64_t(mb) * mb, mb, w.evecs,
+                                             w.evecs_prev, mb, w.xp, w.axp, n, w.active);
+      TNX_LAUNCH_CHECK();
       bcopy_kernel<<<dim3(vchunks, B), BT, 0, st>>>(w.x, n, w.V, sVB, n, w.active);
       TNX_LAUNCH_CHECK();
       bcopy_kernel<<<dim3(vchunks, B), BT, 0, st>>>(w.ax, n, w.AV, sVB, n, w.active);
       TNX_LAUNCH_CHECK();
-      brestart_kernel<<<(B + 255) / 256, 256, 0, st>>>(w.Hm, int64_t(mb) * mb, w.evals, w.evecs, mb, B, w.active);
+      bcopy_kernel<<<dim3(vchunks, B), BT, 0, st>>>(w.xp, n, w.V + n, sVB, n, w.active);
       TNX_LAUNCH_CHECK();
-      k = 1;
+      bcopy_kernel<<<dim3(vchunks, B), BT, 0, st>>>(w.axp, n, w.AV + n, sVB, n, w.active);
+      TNX_LAUNCH_CHECK();
+      bset_theta_kernel<<<(B + 255) / 256, 256, 0, st>>>(w.Hm, int64_t(mb) * mb, w.evals, B, w.active);
+      TNX_LAUNCH_CHECK();
+      k = 2;
     }
   }
   // results: the last Ritz pair of every chain (frozen when its chain retired)

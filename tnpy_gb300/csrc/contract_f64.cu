@@ -30,10 +30,12 @@ __global__ void __launch_bounds__(GB_T) gemm_f64_kernel(int64_t M, int64_t N, in
                                                      int64_t sa, const double* __restrict__ B,
                                                      int64_t ldb, int64_t sb, double beta,
                                                      double* __restrict__ C, int64_t ldc,
-                                                     int64_t sc, int64_t k_total) {
+                                                     int64_t sc, int64_t k_total,
+                                                     const int* __restrict__ bmask) {
   __shared__ double As[GB_K][GB_M + 1];
   __shared__ double Bs[GB_K][GB_N + 1];
   const int64_t bz = blockIdx.z;
+  if (bmask && !bmask[bz]) return;  // a batch entry the caller masked out
   A += bz * sa;
   B += bz * sb;
   C += bz * sc;
@@ -118,7 +120,8 @@ __global__ void __launch_bounds__(GB_T) gemm_f64_kernel(int64_t M, int64_t N, in
 
 int gemm_f64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
              int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta,
-             double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total) {
+             double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total,
+             const int* bmask) {
   if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
   if (k <= 0) {
     // C = beta * C; only the beta == 0 case is used here
@@ -132,13 +135,17 @@ int gemm_f64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, co
   TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_f64: m too large");
   profile_mark(KF_F64_GEMM, st, true);
   if (!ta && !tb)
-    gemm_f64_kernel<false, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+    gemm_f64_kernel<false, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total,
+                                                          bmask);
   else if (ta && !tb)
-    gemm_f64_kernel<true, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+    gemm_f64_kernel<true, false><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total,
+                                                          bmask);
   else if (!ta && tb)
-    gemm_f64_kernel<false, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+    gemm_f64_kernel<false, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total,
+                                                          bmask);
   else
-    gemm_f64_kernel<true, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+    gemm_f64_kernel<true, true><<<grid, GB_T, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total,
+                                                          bmask);
   profile_mark(KF_F64_GEMM, st, false);
   profile_work(KF_F64_GEMM, 2.0 * double(m) * n * k * batch, 8.0 * (double(m) * k + double(k) * n + double(m) * n) * batch);
   TNX_LAUNCH_CHECK();

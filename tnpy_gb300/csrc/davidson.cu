@@ -211,6 +211,65 @@ __global__ void __launch_bounds__(DT) ritz_kernel(const T* __restrict__ V, const
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
+// generalised form: x = V s, ax = AV s, bx = BV s, r = ax - theta bx,
+// t = r / (diagA - theta diagB), partial ||r||^2 (FP64)
+__global__ void __launch_bounds__(DT) gritz_kernel(const double* __restrict__ V, const double* __restrict__ AV,
+                                                  const double* __restrict__ BV, int64_t ldv, int k,
+                                                  const double* __restrict__ s, const double* __restrict__ theta_p,
+                                                  const double* __restrict__ da, const double* __restrict__ db,
+                                                  double* __restrict__ x, double* __restrict__ ax,
+                                                  double* __restrict__ bx, double* __restrict__ t, int64_t n,
+                                                  double* __restrict__ part, int nchunk) {
+  __shared__ double sh[DT / 32];
+  __shared__ double ss[MAXB];
+  if (threadIdx.x < k) ss[threadIdx.x] = s[threadIdx.x];
+  __syncthreads();
+  const double theta = theta_p[0];
+  double nrm = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(nchunk) * DT) {
+    double xv = 0.0, av = 0.0, bv = 0.0;
+    for (int j = 0; j < k; ++j) {
+      xv = fma(ss[j], V[int64_t(j) * ldv + i], xv);
+      av = fma(ss[j], AV[int64_t(j) * ldv + i], av);
+      bv = fma(ss[j], BV[int64_t(j) * ldv + i], bv);
+    }
+    const double r = av - theta * bv;
+    x[i] = xv;
+    ax[i] = av;
+    bx[i] = bv;
+    double den = da[i] - theta * db[i];
+    if (fabs(den) < 1e-2) den = den >= 0.0 ? 1e-2 : -1e-2;
+    t[i] = r / den;
+    nrm = fma(r, r, nrm);
+  }
+  const double tot = block_sum(nrm, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// w2 -= sum_{j<k} h[j] V2[j] (the B-images follow the same combination as the vectors)
+__global__ void __launch_bounds__(DT) axpy_basis_kernel(const double* __restrict__ V2, int64_t ldv, int k,
+                                                       const double* __restrict__ h, double* __restrict__ w2,
+                                                       int64_t n) {
+  __shared__ double hs[MAXB];
+  if (threadIdx.x < k) hs[threadIdx.x] = h[threadIdx.x];
+  __syncthreads();
+  for (int64_t i = int64_t(blockIdx.x) * DT + threadIdx.x; i < n; i += int64_t(gridDim.x) * DT) {
+    double acc = w2[i];
+    for (int j = 0; j < k; ++j) acc = fma(-hs[j], V2[int64_t(j) * ldv + i], acc);
+    w2[i] = acc;
+  }
+}
+
+// w *= 1/sqrt(nrm2[0]) for two vectors at once
+__global__ void scale2_kernel(double* __restrict__ w, double* __restrict__ w2, int64_t n,
+                              const double* __restrict__ nrm2) {
+  const double s = 1.0 / sqrt(nrm2[0]);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    w[i] *= s;
+    w2[i] *= s;
+  }
+}
+
 // after a restart to the single Ritz vector x: H = [[theta]], Ritz coefficients s = [1]
 __global__ void restart_kernel(double* Hm, const double* evals, double* evecs) {
   Hm[0] = evals[0];
@@ -704,6 +763,174 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   return TNX_OK;
 }
 
+// ---- generalised problem A x = lambda B x (B symmetric positive definite) ------------------
+// Davidson with a B-orthonormal basis: V^T B V = I, so the projected problem V^T A V s = theta s
+// is standard. Each expansion B-orthogonalises the correction t against V (two classical
+// passes; the B-images BV follow the same combinations, so one B product per expansion), applies
+// A once, and forms x = V s, the residual A x - theta B x and the correction
+// (diag A - theta diag B)^-1 r. Converged when ||A x - theta B x|| <= tol max(1, |theta|), or
+// when the residual has stagnated (no 10 % gain in 40 expansions) below 1e-6 max(1, |theta|):
+// shift-invert pencils converge slowly near their floor, and there the Ritz value is already
+// accurate to ~|r|^2 / gap.
+struct GDavWs {
+  double *V, *AV, *BV, *x, *ax, *bx, *t, *da, *db, *Hm, *evals, *evecs, *part, *scal, *T1, *T2;
+};
+
+size_t gdav_layout(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr, int64_t dl2, int64_t dr2, int mb,
+                   void* base, GDavWs* w) {
+  const int64_t n = chi_l * d * chi_r;
+  const int64_t ne1 = matvec1_scratch_elems(chi_l, d, chi_r, dl, dr);
+  const int64_t ne2 = matvec1_scratch_elems(chi_l, d, chi_r, dl2, dr2);
+  const int64_t ne = ne1 > ne2 ? ne1 : ne2;
+  const int nch = nchunk_for(n);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += align_up(bytes);
+    return o;
+  };
+  size_t oV = take(size_t(mb) * n * 8), oAV = take(size_t(mb) * n * 8), oBV = take(size_t(mb) * n * 8),
+         ox = take(n * 8), oax = take(n * 8), obx = take(n * 8), ot = take(n * 8), oda = take(n * 8),
+         odb = take(n * 8), oH = take(size_t(mb) * mb * 8), oev = take(size_t(mb) * 8),
+         oevec = take(size_t(mb) * mb * 8), opart = take(size_t(mb + 1) * nch * 8), oscal = take(size_t(4 * MAXB) * 8),
+         oT1 = take(ne * 8), oT2 = take(ne * 8);
+  if (w && base) {
+    char* b = static_cast<char*>(base);
+    w->V = reinterpret_cast<double*>(b + oV);
+    w->AV = reinterpret_cast<double*>(b + oAV);
+    w->BV = reinterpret_cast<double*>(b + oBV);
+    w->x = reinterpret_cast<double*>(b + ox);
+    w->ax = reinterpret_cast<double*>(b + oax);
+    w->bx = reinterpret_cast<double*>(b + obx);
+    w->t = reinterpret_cast<double*>(b + ot);
+    w->da = reinterpret_cast<double*>(b + oda);
+    w->db = reinterpret_cast<double*>(b + odb);
+    w->Hm = reinterpret_cast<double*>(b + oH);
+    w->evals = reinterpret_cast<double*>(b + oev);
+    w->evecs = reinterpret_cast<double*>(b + oevec);
+    w->part = reinterpret_cast<double*>(b + opart);
+    w->scal = reinterpret_cast<double*>(b + oscal);
+    w->T1 = reinterpret_cast<double*>(b + oT1);
+    w->T2 = reinterpret_cast<double*>(b + oT2);
+  }
+  return off;
+}
+
+int gdavidson1(const double* L, const double* W, const double* R, const double* L2, const double* W2,
+               const double* R2, double* x_io, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+               int64_t dl2, int64_t dr2, double tol, int max_iter, int mb, int precision, double* eval_out,
+               double* resid_out, int* iters_out, void* ws, size_t ws_bytes, cudaStream_t st) {
+  GDavWs w;
+  const size_t need = gdav_layout(chi_l, d, chi_r, dl, dr, dl2, dr2, mb, ws, &w);
+  if (ws_bytes < need || !ws) {
+    set_error("tnx_gdavidson1: workspace %zu bytes < required %zu", ws_bytes, need);
+    return TNX_ERR_WORKSPACE;
+  }
+  const int64_t n = chi_l * d * chi_r;
+  if (mb > n) mb = int(n < 2 ? 2 : n);
+  const int nch = nchunk_for(n);
+  const unsigned sblocks = (unsigned)((n + DT - 1) / DT < 152 * 8 ? (n + DT - 1) / DT : 152 * 8);
+  const bool df = precision != TNX_FP64;
+  auto amul = [&](const double* in, double* out) {
+    return matvec1_f64(L, W, R, in, out, chi_l, d, chi_r, dl, dr, w.T1, w.T2, st, df);
+  };
+  auto bmul = [&](const double* in, double* out) {
+    return matvec1_f64(L2, W2, R2, in, out, chi_l, d, chi_r, dl2, dr2, w.T1, w.T2, st, df);
+  };
+  double* h = w.scal;
+  double* nrm2 = w.scal + MAXB;
+  double* rn2 = w.scal + MAXB + 2;
+  double host[2];
+  TNX_TRY(tnx_diag1(L, W, R, w.da, chi_l, d, chi_r, dl, dr, st));
+  TNX_TRY(tnx_diag1(L2, W2, R2, w.db, chi_l, d, chi_r, dl2, dr2, st));
+  TNX_CUDA(cudaMemcpyAsync(w.t, x_io, n * 8, cudaMemcpyDeviceToDevice, st));
+  int k = 0, iters = 0, best_it = 0;
+  double theta = 0.0, rnorm = INFINITY, best = INFINITY;
+  bool converged = false;
+  for (;;) {
+    double* vk = w.V + int64_t(k) * n;
+    double* bvk = w.BV + int64_t(k) * n;
+    TNX_CUDA(cudaMemcpyAsync(vk, w.t, n * 8, cudaMemcpyDeviceToDevice, st));
+    // pass 1: against V in the B inner product, h_j = (B V_j) . t
+    if (k > 0) {
+      TNX_TRY(dots<double>(w.BV, n, k, vk, n, w.part, h, 1, nullptr, 0, st));
+      update_kernel<double><<<nch, DT, 0, st>>>(w.V, n, k, h, vk, n, w.part, nch, nullptr);
+      TNX_LAUNCH_CHECK();
+    }
+    TNX_TRY(bmul(vk, bvk));
+    ++iters;
+    // pass 2: h_j = V_j . (B t), applied to t and (linearly) to B t
+    if (k > 0) {
+      TNX_TRY(dots<double>(w.V, n, k, bvk, n, w.part, h, 1, nullptr, 0, st));
+      update_kernel<double><<<nch, DT, 0, st>>>(w.V, n, k, h, vk, n, w.part, nch, nullptr);
+      TNX_LAUNCH_CHECK();
+      axpy_basis_kernel<<<sblocks, DT, 0, st>>>(w.BV, n, k, h, bvk, n);
+      TNX_LAUNCH_CHECK();
+    }
+    TNX_TRY(dots<double>(vk, n, 1, bvk, n, w.part, nrm2, 1, nullptr, 0, st));
+    TNX_CUDA(cudaMemcpyAsync(host, nrm2, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaStreamSynchronize(st));
+    if (!(host[0] > 0.0) || !std::isfinite(host[0])) {
+      if (k == 0) {
+        set_error("tnx_gdavidson1: start vector has zero or non-finite B-norm");
+        return TNX_ERR_INVALID_ARG;
+      }
+      break;  // the correction fell into the basis
+    }
+    scale2_kernel<<<sblocks, DT, 0, st>>>(vk, bvk, n, nrm2);
+    TNX_LAUNCH_CHECK();
+    double* avk = w.AV + int64_t(k) * n;
+    TNX_TRY(amul(vk, avk));
+    TNX_TRY(dots<double>(w.V, n, k + 1, avk, n, w.part, w.Hm + k, mb, w.Hm + int64_t(k) * mb, 1, st));
+    ++k;
+    TNX_TRY(rr_lowest_f64(w.Hm, k, mb, w.evals, w.evecs, st));
+    gritz_kernel<<<nch, DT, 0, st>>>(w.V, w.AV, w.BV, n, k, w.evecs, w.evals, w.da, w.db, w.x, w.ax, w.bx, w.t, n,
+                                     w.part, nch);
+    TNX_LAUNCH_CHECK();
+    reduce_kernel<<<1, DT, 0, st>>>(w.part, nch, rn2, 1, nullptr, 0);
+    TNX_LAUNCH_CHECK();
+    TNX_CUDA(cudaMemcpyAsync(host, w.evals, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaMemcpyAsync(host + 1, rn2, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaStreamSynchronize(st));
+    theta = host[0];
+    rnorm = sqrt(fmax(host[1], 0.0));
+    if (!std::isfinite(theta) || !std::isfinite(rnorm)) {
+      set_error("tnx_gdavidson1: non-finite Ritz value or residual");
+      return TNX_ERR_INVALID_ARG;
+    }
+    const double scale = fmax(1.0, fabs(theta));
+    if (rnorm <= tol * scale || k >= n) {
+      converged = true;
+      break;
+    }
+    if (rnorm < 0.9 * best) {
+      best = rnorm;
+      best_it = iters;
+    } else if (iters - best_it >= 40 && rnorm <= 1e-6 * scale) {
+      converged = true;  // stagnated near the floor
+      break;
+    }
+    if (iters >= max_iter) break;
+    if (k == mb) {  // restart to the Ritz vector (B-unit by construction)
+      TNX_CUDA(cudaMemcpyAsync(w.V, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+      TNX_CUDA(cudaMemcpyAsync(w.AV, w.ax, n * 8, cudaMemcpyDeviceToDevice, st));
+      TNX_CUDA(cudaMemcpyAsync(w.BV, w.bx, n * 8, cudaMemcpyDeviceToDevice, st));
+      restart_kernel<<<1, 1, 0, st>>>(w.Hm, w.evals, w.evecs);
+      TNX_LAUNCH_CHECK();
+      k = 1;
+    }
+  }
+  TNX_CUDA(cudaMemcpyAsync(x_io, w.x, n * 8, cudaMemcpyDeviceToDevice, st));
+  if (eval_out) *eval_out = theta;
+  if (resid_out) *resid_out = rnorm;
+  if (iters_out) *iters_out = iters;
+  if (!converged) {
+    set_error("tnx_gdavidson1: %d products, residual %.3e > tol %.3e", iters, rnorm, tol);
+    return TNX_ERR_NOT_CONVERGED;
+  }
+  return TNX_OK;
+}
+
 }  // namespace tnx
 
 using namespace tnx;
@@ -723,6 +950,27 @@ int tnx_davidson1_stats(int* out) {
   out[2] = g_dav_stats.anchors;
   out[3] = g_dav_stats.restarts;
   return TNX_OK;
+}
+
+size_t tnx_gdavidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                                      int64_t dl2, int64_t dr2, int max_basis) {
+  if (max_basis > MAXB) max_basis = MAXB;
+  return gdav_layout(chi_l, d, chi_r, dl, dr, dl2, dr2, max_basis, nullptr, nullptr);
+}
+
+int tnx_gdavidson1(const double* L, const double* W, const double* R, const double* L2, const double* W2,
+                   const double* R2, double* x, int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
+                   int64_t dl2, int64_t dr2, double tol, int max_iter, int max_basis, int precision,
+                   double* eval_out, double* resid_out, int* iters_out, void* workspace, size_t workspace_bytes,
+                   void* stream) {
+  TNX_CHECK_ARG(L && W && R && L2 && W2 && R2 && x, "null pointer");
+  TNX_CHECK_ARG(chi_l > 0 && d > 0 && chi_r > 0 && dl > 0 && dr > 0 && dl2 > 0 && dr2 > 0, "non-positive dimension");
+  TNX_CHECK_ARG(max_basis >= 2 && max_basis <= MAXB, "max_basis must be in [2, %d] (got %d)", MAXB, max_basis);
+  TNX_CHECK_ARG(max_iter >= 1 && tol >= 0.0, "max_iter must be >= 1 and tol >= 0");
+  TNX_CHECK_ARG(precision >= TNX_FP64 && precision <= TNX_DF64, "unknown precision %d", precision);
+  TNX_CHECK_SHAPE(dl * d <= 64 && dr * d <= 64 && dl2 * d <= 64 && dr2 * d <= 64, "MPO bond too large");
+  return gdavidson1(L, W, R, L2, W2, R2, x, chi_l, d, chi_r, dl, dr, dl2, dr2, tol, max_iter, max_basis, precision,
+                    eval_out, resid_out, iters_out, workspace, workspace_bytes, as_stream(stream));
 }
 
 int tnx_davidson1(const double* L, const double* W, const double* R, double* x, int64_t chi_l, int64_t d,

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(NT) gemm_df64_kernel(int64_t M, int64_t N, int
                                                      const double* __restrict__ A, int64_t lda, int64_t sa,
                                                      const double* __restrict__ B, int64_t ldb, int64_t sb,
                                                      double beta, double* __restrict__ C, int64_t ldc, int64_t sc,
-                                                     int64_t k_total) {
+                                                     int64_t k_total, const int* __restrict__ bmask) {
   constexpr int DM = BM, DN = BN, DT = NT, TY = NT / 16;
   constexpr int RI = DM / TY, RJ = DN / 16;  // outputs per thread
   static_assert(NT % 16 == 0 && DM % TY == 0 && DN % 16 == 0 && (DM * DK) % NT == 0 && (DN * DK) % NT == 0,
@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(NT) gemm_df64_kernel(int64_t M, int64_t N, int
   __shared__ float Ah[DK][DM + 4], Al[DK][DM + 4];
   __shared__ float Bh[DK][DN + 4], Bl[DK][DN + 4];
   const int64_t bz = blockIdx.z;
+  if (bmask && !bmask[bz]) return;  // a batch entry the caller masked out
   A += bz * sa;
   B += bz * sb;
   C += bz * sc;
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(NT) gemm_df64_kernel(int64_t M, int64_t N, int
 
 int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
               int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C, int64_t ldc, int64_t sc,
-              int64_t batch, cudaStream_t st, int64_t k_total) {
+              int64_t batch, cudaStream_t st, int64_t k_total, const int* bmask) {
   if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
   if (k <= 0) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st);
   TNX_CHECK_SHAPE(batch <= 65535, "gemm_df64: batch %lld > 65535", (long long)batch);
@@ -168,7 +169,7 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
     dim3 grid((unsigned)((n + bn - 1) / bn), (unsigned)((m + bm - 1) / bm), (unsigned)batch);
     TNX_CHECK_SHAPE(grid.y <= 65535, "gemm_df64: m too large");
     auto go = [&](auto kernel, int nt) {
-      kernel<<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total);
+      kernel<<<grid, nt, 0, st>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, k_total, bmask);
     };
     if (small) {
       if (!ta && !tb) go(gemm_df64_kernel<false, false, 32, 32, 64>, 64);
@@ -186,7 +187,8 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
   };
   profile_mark(KF_F64_GEMM, st, true);
   const TuneKey key{1, int64_t(ta) * 2 + int64_t(tb), m, n, k_total > 0 ? k_total : k, batch};
-  TNX_TRY(autotuned(key, 2, small_rule ? 1 : 0, beta == 0.0, st, launch));
+  // a masked call skips some batch entries: its timing would not represent the shape
+  TNX_TRY(autotuned(key, 2, small_rule ? 1 : 0, beta == 0.0 && !bmask, st, launch));
   profile_mark(KF_F64_GEMM, st, false);
   profile_work(KF_F64_GEMM, 2.0 * double(m) * n * (k_total > 0 ? k_total : k * batch),
                8.0 * (double(m) * k + double(k) * n + double(m) * n) * batch);
@@ -195,9 +197,10 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
 
 int gemm_fp64_class(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                     int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C,
-                    int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total) {
-  if (df) return gemm_df64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st, k_total);
-  return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st, k_total);
+                    int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total, const int* bmask) {
+  if (df)
+    return gemm_df64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st, k_total, bmask);
+  return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, st, k_total, bmask);
 }
 
 }  // namespace tnx

@@ -153,11 +153,12 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
 }
 
 // ---- FP64 GEMM (row-major, optional transposes, strided batch) --------------------
-// k_total > 0 selects split-K: batch z multiplies the K slice [z*k, min((z+1)*k, k_total))
+// k_total > 0 selects split-K: batch z multiplies the K slice [z*k, min((z+1)*k, k_total));
+// bmask (device, batch ints, may be null) skips the batch entries whose mask is 0
 int gemm_f64(bool trans_a, bool trans_b, int64_t m, int64_t n, int64_t k, double alpha,
              const double* A, int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb,
              double beta, double* C, int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st,
-             int64_t k_total = 0);
+             int64_t k_total = 0, const int* bmask = nullptr);
 // C = alpha * op(A) op(B) + beta * C with K split over nsplit CTAs layers; part holds
 // nsplit * m * n doubles of partial products
 int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
@@ -166,7 +167,7 @@ int gemm_f64_splitk(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double al
 // double-FP32 emulated GEMM (same contract as gemm_f64)
 int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
               int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C, int64_t ldc, int64_t sc,
-              int64_t batch, cudaStream_t st, int64_t k_total = 0);
+              int64_t batch, cudaStream_t st, int64_t k_total = 0, const int* bmask = nullptr);
 // FP64-class GEMM on the tensor cores (Ozaki slicing, gemm_oz.cu); workspace sized by
 // gemm_oz_workspace_bytes(m, n, k)
 size_t gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k);
@@ -176,7 +177,8 @@ int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, con
 // df = true: double-FP32 emulation; false: native FP64
 int gemm_fp64_class(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                     int64_t lda, int64_t sa, const double* B, int64_t ldb, int64_t sb, double beta, double* C,
-                    int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total = 0);
+                    int64_t ldc, int64_t sc, int64_t batch, cudaStream_t st, int64_t k_total = 0,
+                    const int* bmask = nullptr);
 
 // ---- MPO contraction steps ---------------------------------------------------------
 // T2[(a',s'),(c,v)] = sum_{w,s} T1[(w,a'),(s,c)] W[w,v,s,s']   (left / matvec form)

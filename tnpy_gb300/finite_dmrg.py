@@ -286,6 +286,110 @@ class FiniteDMRG:
         return MatrixProductStateMeasurements(self.mps)
 
 
+class ShiftInvertDMRG(FiniteDMRG):
+    """Shift-invert one-site DMRG for excited states near an energy eps (tnpy/finite_dmrg.py:266-407).
+
+    ``mpo`` is the MPO of H - eps (e.g. RandomHeisenberg(..., offset=eps)); every site solves the
+    generalised problem (H - eps) phi = lambda (H - eps)^2 phi for the smallest lambda, with the
+    second operator from environments of the MPO square (bond D^2): densely below
+    ``exact_solver_dim`` elements (B^-1/2 A B^-1/2 from the device Jacobi eigensolver), else by
+    the device generalised Davidson (tnx_gdavidson1, B-orthonormal basis). ``run`` returns the
+    energies 1/lambda + offset of every sweep and restores psi = (H - eps) phi site by site
+    (tnx_mpo_apply_site); ``measurements`` and ``variance`` act on the restored state."""
+
+    def __init__(self, mpo: MatrixProductOperator, bond_dim: int | None = None, offset: float = 0.0,
+                 block_size: int = 1, mps: MatrixProductState | None = None, exact_solver_dim: int = 200, *,
+                 chi: int | None = None, precision: str = "fp64", seed: int | None = 1234, max_iter: int = 400,
+                 max_basis: int = 48, device=None):
+        if precision == "mixed":
+            raise ValueError("shift-invert DMRG runs in 'fp64' or the FP64-class 'df64' form")
+        super().__init__(mpo, bond_dim, block_size, mps, exact_solver_dim, chi=chi, precision=precision, seed=seed,
+                         max_iter=max_iter, max_basis=max_basis, compute_variance=False, device=device)
+        self._env2 = Environment(mpo=mpo.square(), mps=self.mps, precision=precision)
+        self._offset = float(offset)
+        self._restored_mps: MatrixProductState | None = None
+
+    @property
+    def offset(self) -> float:
+        return self._offset
+
+    @property
+    def restored_mps(self) -> MatrixProductState | None:
+        return self._restored_mps
+
+    def _restore_mps(self):
+        """psi = (H - eps) phi: each site tensor contracted with its MPO tensor (:314-343)."""
+        ws = self._env.mpo.device_tensors(self.mps.device)
+        self._restored_mps = MatrixProductState([K.mpo_apply_site(a, w) for a, w in zip(self.mps.tensors, ws)],
+                                                device=self.mps.device)
+
+    def one_site_solver(self, site: int, tol: float = 1e-8, **kwargs):
+        """Smallest generalised eigenpair at ``site`` (:345-363); the vector is B-normalised."""
+        x = self.mps.tensors[site]
+        if x.numel() < self._exact_solver_dim:
+            self.stats["dense_solves"] += 1
+            a = self._env.one_site_full_matrix(site)
+            b = self._env2.one_site_full_matrix(site)
+            n = a.shape[0]
+            wb, ub = K.eigh_batched([(0.5 * (b + b.T)).contiguous()], keep=n)
+            ub = ub[0, :n, :]
+            if float(wb.min().item()) <= 0.0:
+                raise RuntimeError(f"site {site}: the squared operator is not positive definite")
+            bih = K.gemm((ub * wb[0].rsqrt()[None, :]).contiguous(), ub, trans_b=True)  # B^-1/2
+            c = K.gemm(bih, K.gemm(a, bih))
+            wc, uc = K.eigh_batched([(0.5 * (c + c.T)).contiguous()], keep=1)
+            vec = K.gemm(bih, uc[0, :n, :].contiguous())
+            return float(wc[0, 0].item()), vec.reshape(x.shape).contiguous()
+        self.stats["iterative_solves"] += 1
+        psi = x.clone()
+        L, W, R = self._env.site_operator(site)
+        L2, W2, R2 = self._env2.site_operator(site)
+        e, rn, its, ok = K.gdavidson1(L, W, R, L2, W2, R2, psi, tol=tol,
+                                      max_iter=kwargs.get("max_iter", self.max_iter),
+                                      max_basis=kwargs.get("max_basis", self.max_basis), precision=self.precision)
+        self.stats["matvecs"] += its
+        if not ok:
+            self.stats["unconverged"] += 1
+            logger.warning(f"site {site}: generalised Davidson did not converge (residual {rn:.3e}, {its} expansions)")
+        return e, psi
+
+    def sweep(self, direction: Direction = Direction.RIGHTWARD, tol: float = 1e-8, **kwargs) -> float | None:
+        """:365-384: the FiniteDMRG site update, plus the MPO-square environments."""
+        sites = range(self.n_sites - 1) if direction == Direction.RIGHTWARD else range(self.n_sites - 1, 0, -1)
+        energy = None
+        for site in sites:
+            energy, psi = self.one_site_solver(site, tol, **kwargs)
+            logger.debug(f"Sweeping to site [{site + 1}/{self.n_sites}], E0 = {1 / energy + self._offset}")
+            self._env.update_mps(site, psi)
+            self.perturb_wave_function(site)
+            self._env.split_tensor(site, direction=direction)
+            self._env.update(site, direction=direction)
+            self._env2.update(site, direction=direction)
+        return energy
+
+    def run(self, tol: float = 1e-7, max_sweep: int = 100, metric: Metric = Metric.ENERGY, **kwargs) -> list[float]:
+        """:386-395: sweeps on lambda, then 1/lambda + offset and the restored state."""
+        lam = super().run(tol, max_sweep, metric, **kwargs)
+        self._restore_mps()
+        return (np.reciprocal(np.asarray(lam, dtype=float)) + self._offset).tolist()
+
+    update = run
+
+    @property
+    def measurements(self) -> MatrixProductStateMeasurements:
+        if len(self._energies) == 1:
+            raise RuntimeError("FiniteDMRG is probably not executed yet.")
+        return MatrixProductStateMeasurements(self.restored_mps)
+
+    def variance(self) -> float:
+        """<psi_r|(H - eps)^2|psi_r> - lambda^2 - offset^2 on the restored (unnormalised) state, as
+        the reference computes it (:403-407)."""
+        from .matrix_product_state import expectation_value
+
+        return expectation_value(self.restored_mps, self._env.mpo.square()) - self._energies[-1] ** 2 - \
+            self._offset ** 2
+
+
 class BatchedFiniteDMRG:
     """Many independent chains of one shape (disorder realisations, parameter scans) swept in
     lockstep, every kernel spanning all chains: FiniteDMRG.run (finite_dmrg.py:214-257) per chain,

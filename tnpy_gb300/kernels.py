@@ -124,6 +124,39 @@ def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64"
     return ev.value, rn.value, it.value, converged
 
 
+def gdavidson1(L, W, R, L2, W2, R2, x, tol=1e-8, max_iter=400, max_basis=24, precision="fp64"):
+    """Lowest eigenpair of A x = lambda B x with A = H_eff(L, W, R), B = H_eff(L2, W2, R2)
+    (B positive definite) from x (overwritten with the B-unit eigenvector).
+    Returns (eigenvalue, residual norm, expansions, converged)."""
+    L, W, R, L2, W2, R2 = (_f64(t, n) for t, n in ((L, "L"), (W, "W"), (R, "R"), (L2, "L2"), (W2, "W2"), (R2, "R2")))
+    if x.dtype != torch.float64 or not x.is_cuda or not x.is_contiguous():
+        raise ValueError("x must be a contiguous float64 CUDA tensor (it is overwritten)")
+    chi_l, d, chi_r, dl, dr = _site_dims(L, W, R)
+    chi_l2, d2, chi_r2, dl2, dr2 = _site_dims(L2, W2, R2)
+    if (chi_l2, d2, chi_r2) != (chi_l, d, chi_r):
+        raise ValueError("the two operators act on different site shapes")
+    p = precision_code(precision)
+    wp, wn = Workspace.get(lib.tnx_gdavidson1_workspace_bytes(chi_l, d, chi_r, dl, dr, dl2, dr2, max_basis), x.device)
+    ev, rn, it = ctypes.c_double(0.0), ctypes.c_double(0.0), ctypes.c_int(0)
+    st = lib.tnx_gdavidson1(ptr(L), ptr(W), ptr(R), ptr(L2), ptr(W2), ptr(R2), ptr(x), chi_l, d, chi_r, dl, dr, dl2,
+                            dr2, float(tol), int(max_iter), int(max_basis), p, ctypes.byref(ev), ctypes.byref(rn),
+                            ctypes.byref(it), wp, wn, stream_ptr())
+    if st not in (_lib.TNX_OK, _lib.TNX_ERR_NOT_CONVERGED):
+        check("tnx_gdavidson1", st)
+    return ev.value, rn.value, it.value, st == _lib.TNX_OK
+
+
+def mpo_apply_site(A: torch.Tensor, W: torch.Tensor) -> torch.Tensor:
+    """out[(a w), k, (c v)] = sum_b W[w, v, k, b] A[a, b, c]: one site of O|psi>."""
+    A, W = _f64(A, "A"), _f64(W, "W")
+    chi_l, d, chi_r = A.shape
+    dl, dr = W.shape[0], W.shape[1]
+    out = torch.empty((chi_l * dl, d, chi_r * dr), dtype=torch.float64, device=A.device)
+    check("tnx_mpo_apply_site", lib.tnx_mpo_apply_site(ptr(A), ptr(W), ptr(out), chi_l, d, chi_r, dl, dr,
+                                                       stream_ptr()))
+    return out
+
+
 def davidson1_stats() -> dict:
     """Counters of this thread's last davidson1 call: first-phase matvecs, anchored-phase
     matvecs (mixed form), FP64-class anchor products and thick restarts."""
