@@ -294,15 +294,17 @@ def test_gauge_move_df64(cuda):
     np.testing.assert_allclose(np.tensordot(a2, nb2, axes=([2], [0])), two, atol=1e-11)
 
 
+@pytest.mark.parametrize("chi", [512, 1024])
 @pytest.mark.parametrize("direction", [1, -1])
-def test_gauge_move_df64_rank_deficient(cuda, direction):
-    """chi=512 gauge move in the FP64-class (double-FP32) form on a site tensor whose Schmidt
-    values span 20 decades, as converged MPS bonds do: Q stays orthonormal to 1e-12 and the
-    two-site product is reproduced to 1e-11 of its norm."""
+def test_gauge_move_df64_rank_deficient(cuda, direction, chi):
+    """chi=512 and 1024 gauge moves in the FP64-class form (double-FP32 panels, Q from the
+    compact WY form on the tensor cores) on a site tensor whose Schmidt values span 20 decades,
+    as converged MPS bonds do: Q stays orthonormal to 1e-12 and the two-site product is
+    reproduced to 1e-11 of its norm."""
     import tnpy_gb300.kernels as K
 
     rng = np.random.RandomState(5)
-    chi, d = 512, 2
+    d = 2
     if direction == 1:
         m, n = chi * d, chi
     else:

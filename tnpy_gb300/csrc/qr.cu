@@ -13,8 +13,9 @@
 // the compact-WY T factor; FP64 here, double-FP32 in qr_panel_df.cuh for the FP64-class
 // modes; one-CTA kernel for panels too tall for a cluster), the trailing matrix is updated
 // with three FP64 / double-FP32 GEMMs (W = V^T C, W = T^T W, C -= V W) with look-ahead (the
-// next panel's columns first, the rest on a second stream), and Q is formed by applying the
-// panels backwards to [I; 0].
+// next panel's columns first, the rest on a second stream). Q is formed by applying the panels
+// backwards to [I; 0], or, in the FP64-class modes at large bonds, from the compact WY form of
+// all reflectors with four FP64-class tensor-core GEMMs (form_q_wy).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -429,6 +430,17 @@ unsigned blocks_for(int64_t total) {
   return unsigned(b < 1 ? 1 : b);
 }
 
+// Tf (row-major n x n): the panel T factors (column-major NB x NB each, in T) on the diagonal
+// blocks, zero elsewhere
+__global__ void t_diag_kernel(const double* __restrict__ T, int64_t n, int NB, double* __restrict__ Tf) {
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < n * n; e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = e / n, c = e % n, p = r / NB;
+    double v = 0.0;
+    if (r <= c && c / NB == p) v = T[p * NB * NB + (c - p * NB) * NB + (r - p * NB)];
+    Tf[e] = v;
+  }
+}
+
 // Two scratch sets (Vp / W1 / W2 / part): set 0 for the caller's stream, set 1 for the
 // look-ahead stream of the factorisation.
 struct QrWs {
@@ -627,6 +639,127 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
   return rc;
 }
 
+// ---- next-panel update in double-FP32, three short launches (FP64-class modes) ----------
+//
+// The update of the next panel's columns by H_p sits on the factorisation's critical path
+// between two panels. As three general GEMM launches (split-K V^T C with its reduction, T^T W,
+// C -= V W) it is latency-bound at 64 x 64 x (m - j0); these kernels spread each phase over
+// all rows of the GPU instead: NR_ROWS-row chunks of V^T C per CTA, a fixed-order reduction of
+// the chunk partials fused with T^T W, and the rank-nb update per row chunk.
+constexpr int NR_ROWS = 16;   // rows of V and C per CTA in the partial and update kernels
+constexpr int NR_T = 256;     // threads of those kernels
+
+// part[c][a][b] = sum over rows r of chunk c of V[r][a] C[r][b]  (a < nb, b < nc <= 64; df2)
+__global__ void __launch_bounds__(NR_T) nar_partial_kernel(const double* __restrict__ Vp, int64_t mp, int nb,
+                                                           const double* __restrict__ C, int64_t ldc, int nc,
+                                                           qrdf::df2* __restrict__ part) {
+  __shared__ qrdf::df2 Vs[NR_ROWS][64], Cs[NR_ROWS][64];
+  const int tid = threadIdx.x;
+  const int64_t r0 = int64_t(blockIdx.x) * NR_ROWS;
+  for (int e = tid; e < NR_ROWS * 64; e += NR_T) {
+    const int r = e % NR_ROWS, c = e / NR_ROWS;
+    const int64_t gr = r0 + r;
+    qrdf::df2 v = {0.f, 0.f}, x = {0.f, 0.f};
+    if (gr < mp) {
+      if (c < nb) split_df(Vp[int64_t(c) * mp + gr], v.h, v.l);
+      if (c < nc) split_df(C[int64_t(c) * ldc + gr], x.h, x.l);
+    }
+    Vs[r][c] = v;
+    Cs[r][c] = x;
+  }
+  __syncthreads();
+  const int a = tid & 63, bq = tid >> 6;  // outputs (a, bq + 4 j)
+  qrdf::df2 acc[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j] = {0.f, 0.f};
+#pragma unroll 4
+  for (int r = 0; r < NR_ROWS; ++r) {
+    const qrdf::df2 v = Vs[r][a];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) qrdf::acc(acc[j], v, Cs[r][bq + 4 * j]);
+  }
+  qrdf::df2* out = part + int64_t(blockIdx.x) * 64 * 64;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) out[a * 64 + bq + 4 * j] = qrdf::norm(acc[j]);
+}
+
+// W2[a][b] = sum_k T(k, a) W[k][b], W[k][b] = sum over chunks of part[c][k][b] in chunk order;
+// one CTA of 64 threads per column b; T column-major (ld NB), upper triangular
+__global__ void __launch_bounds__(64) nar_reduce_kernel(const qrdf::df2* __restrict__ part, int nchunk, int nb,
+                                                        const double* __restrict__ T, int NB,
+                                                        qrdf::df2* __restrict__ W2) {
+  __shared__ qrdf::df2 Ws[64];
+  const int b = blockIdx.x, k = threadIdx.x;
+  qrdf::df2 s = {0.f, 0.f};
+  for (int c = 0; c < nchunk; ++c) s = qrdf::add(s, part[int64_t(c) * 64 * 64 + k * 64 + b]);
+  Ws[k] = s;
+  __syncthreads();
+  const int a = threadIdx.x;
+  qrdf::df2 t = {0.f, 0.f};
+  if (a < nb)
+    for (int kk = 0; kk <= a; ++kk) {
+      qrdf::df2 tk;
+      split_df(T[a * NB + kk], tk.h, tk.l);
+      qrdf::acc(t, tk, Ws[kk]);
+    }
+  W2[a * 64 + b] = qrdf::norm(t);
+}
+
+// C[r][b] -= sum_a V[r][a] W2[a][b] for the rows of one chunk
+__global__ void __launch_bounds__(NR_T) nar_update_kernel(const double* __restrict__ Vp, int64_t mp, int nb,
+                                                          const qrdf::df2* __restrict__ W2, double* __restrict__ C,
+                                                          int64_t ldc, int nc) {
+  __shared__ qrdf::df2 Ws[64][65], Vs[NR_ROWS][65];
+  const int tid = threadIdx.x;
+  const int64_t r0 = int64_t(blockIdx.x) * NR_ROWS;
+  for (int e = tid; e < 64 * 64; e += NR_T) Ws[e / 64][e % 64] = W2[e];
+  for (int e = tid; e < NR_ROWS * 64; e += NR_T) {
+    const int r = e % NR_ROWS, c = e / NR_ROWS;
+    const int64_t gr = r0 + r;
+    qrdf::df2 v = {0.f, 0.f};
+    if (gr < mp && c < nb) split_df(Vp[int64_t(c) * mp + gr], v.h, v.l);
+    Vs[r][c] = v;
+  }
+  __syncthreads();
+  const int r = tid % NR_ROWS, bq = tid / NR_ROWS;  // outputs (r, bq + 16 j)
+  qrdf::df2 acc[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) acc[j] = {0.f, 0.f};
+  for (int a = 0; a < nb; ++a) {
+    const qrdf::df2 v = Vs[r][a];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) qrdf::acc(acc[j], v, Ws[a][bq + 16 * j]);
+  }
+  const int64_t gr = r0 + r;
+  if (gr < mp)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int b = bq + 16 * j;
+      if (b < nc) {
+        const qrdf::df2 s = qrdf::norm(acc[j]);
+        C[int64_t(b) * ldc + gr] -= join_df(s.h, s.l);
+      }
+    }
+}
+
+// C -= V T^T V^T C for a block of nc <= 64 columns (the next panel), double-FP32 arithmetic;
+// part holds ceil(mp / NR_ROWS) * 64 * 64 float pairs, W2 64 * 64
+int apply_panel_narrow(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int nc,
+                       qrdf::df2* W2, qrdf::df2* part, cudaStream_t st) {
+  const int nchunk = int((mp + NR_ROWS - 1) / NR_ROWS);
+  profile_mark(KF_F64_GEMM, st, true);
+  nar_partial_kernel<<<nchunk, NR_T, 0, st>>>(Vp, mp, nb, C, m, nc, part);
+  TNX_LAUNCH_CHECK();
+  nar_reduce_kernel<<<nc, 64, 0, st>>>(part, nchunk, nb, Tp, NB, W2);
+  TNX_LAUNCH_CHECK();
+  nar_update_kernel<<<nchunk, NR_T, 0, st>>>(Vp, mp, nb, W2, C, m, nc);
+  TNX_LAUNCH_CHECK();
+  profile_mark(KF_F64_GEMM, st, false);
+  profile_work(KF_F64_GEMM, 4.0 * double(mp) * nb * nc + 2.0 * double(nb) * nb * nc,
+               8.0 * (2.0 * mp * nb + 2.0 * mp * nc));
+  return TNX_OK;
+}
+
 // C -= V T^T V^T C for the mp x nc column-major block C (ld m): the trailing update of one
 // panel (V: mp x nb column-major in Vp, T: column-major ld NB)
 int apply_panel_t(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int64_t nc,
@@ -675,7 +808,7 @@ int look_ahead(LookAhead** out) {
 // all columns beyond panel p+1 (the bulk of the flops); the 16 SMs of a panel no longer leave
 // the rest of the GPU idle. Panel p+2's columns (part of that bulk) are used only after the
 // look-ahead stream's update of step p has completed. V is double-buffered between the streams.
-int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false) {
+int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false, bool form_q = true) {
   const PanelPlan pp = plan_panels(m, df);
   const int NB = pp.nb;
   const int64_t np = (n + NB - 1) / NB;
@@ -704,7 +837,13 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
       TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, part_cap,
                             la->aux, df));
     }
-    TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, st, df));
+    const bool narrow = df && n >= 64 && (mp + NR_ROWS - 1) / NR_ROWS * 64 * 64 <= part_cap;
+    if (narrow) {
+      TNX_TRY(apply_panel_narrow(m, mp, nb, NB, Vp, Tp, Cn, nb1, reinterpret_cast<qrdf::df2*>(w.W2),
+                                 reinterpret_cast<qrdf::df2*>(w.part), st));
+    } else {
+      TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, st, df));
+    }
     TNX_TRY(factor_panel(pp, w.F, m, j0 + nb, nb1, w.tau + (p + 1) * NB, w.T + (p + 1) * NB * NB, st));
     if (rest > 0) {
       // the next step reads panel p+2's columns and rewrites the other V buffer
@@ -715,6 +854,7 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
   // join the look-ahead stream back (also when it received no work: keeps stream capture balanced)
   TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));
   TNX_CUDA(cudaStreamWaitEvent(st, la->ev_r, 0));
+  if (!form_q) return TNX_OK;
   // Q = H_0 H_1 ... [I; 0]: apply panels last to first to the columns >= j0
   eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.Qc, m, n);
   TNX_LAUNCH_CHECK();
@@ -733,6 +873,108 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false)
     TNX_TRY(gemm_fp64_class(df, true, false, nb, nq, nb, 1.0, Tp, NB, 0, w.W1, nq, 0, 0.0, w.W2, nq, 0, 1, st));
     // Qs -= V W2
     TNX_TRY(gemm_fp64_class(df, true, false, nq, mp, nb, -1.0, w.W2, nq, 0, w.Vp, mp, 0, 1.0, Qs, m, 0, 1, st));
+  }
+  return TNX_OK;
+}
+
+// ---- Q from the compact WY form of all n reflectors (FP64-class modes, large QRs) ----------
+//
+// H_0 H_1 ... H_{n-1} = I - V Tf V^T with V (m x n, unit lower trapezoidal) and Tf (n x n, upper
+// triangular). Tf is assembled from the panel T factors by the block recurrence
+//   Tf = [[T_A, -T_A (V_A^T V_B) T_B], [0, T_B]]
+// applied to pairs of neighbouring blocks of doubling width (64, 128, 256, 512), with the Gram
+// matrix S = V^T V from one FP64-class tensor-core GEMM. Then
+//   Q = [I; 0] - V (Tf V_top^T),   V_top = rows 0..n-1 of V,
+// two more GEMMs. Every product with more than 2^27 multiply-adds runs on the Ozaki GEMM; the
+// backward accumulation it replaces is 16 steps of narrow K = 64 products on the FP32 pipe.
+struct WyWs {
+  double *V, *S, *Tf, *X, *Y;
+  void* oz;
+  size_t oz_bytes;
+};
+
+inline bool wy_applies(int64_t m, int64_t n, bool df) { return df && use_oz(n, n, m) && n >= 256; }
+
+size_t wy_oz_bytes(int64_t m, int64_t n) {
+  size_t b = gemm_oz_workspace_bytes(n, n, m);  // S
+  auto mx = [&](size_t x) { b = x > b ? x : b; };
+  mx(gemm_oz_workspace_bytes(n, n, n));  // X
+  mx(gemm_oz_workspace_bytes(m, n, n));  // Q, row-major output
+  mx(gemm_oz_workspace_bytes(n, m, n));  // Q, column-major output
+  return b;
+}
+
+size_t wy_layout(int64_t m, int64_t n, void* base, WyWs* w) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += align_up(bytes); return o; };
+  const size_t oV = take(size_t(m) * n * 8), oS = take(size_t(n) * n * 8), oT = take(size_t(n) * n * 8),
+               oX = take(size_t(n) * n * 8), oY = take(size_t(n) * n * 8 / 4), obz = wy_oz_bytes(m, n),
+               oZ = take(obz);
+  if (w && base) {
+    char* b = static_cast<char*>(base);
+    w->V = reinterpret_cast<double*>(b + oV);
+    w->S = reinterpret_cast<double*>(b + oS);
+    w->Tf = reinterpret_cast<double*>(b + oT);
+    w->X = reinterpret_cast<double*>(b + oX);
+    w->Y = reinterpret_cast<double*>(b + oY);
+    w->oz = b + oZ;
+    w->oz_bytes = obz;
+  }
+  return off;
+}
+
+// Q (m x n) from the factorisation in w.F / w.T: row-major (ld n) when q_rowmajor, otherwise
+// column-major (ld m)
+int form_q_wy(int64_t m, int64_t n, int NB, const QrWs& w, const WyWs& y, double* Q, bool q_rowmajor,
+              cudaStream_t st) {
+  // V column-major (ld m): row-major view V^T (n x m, ld m)
+  panel_v_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.F, m, 0, int(n), y.V);
+  TNX_LAUNCH_CHECK();
+  t_diag_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.T, n, NB, y.Tf);
+  TNX_LAUNCH_CHECK();
+  // S = V^T V (row-major n x n)
+  TNX_TRY(gemm_fp64_class_oz(true, false, true, n, n, m, 1.0, y.V, m, y.V, m, 0.0, y.S, n, y.oz, y.oz_bytes, st));
+  // Tf_AB = -Tf_A S_AB Tf_B for neighbouring blocks A = [a0, a0 + b), B = [a0 + b, a0 + 2b)
+  for (int64_t b = NB; b < n; b *= 2) {
+    const int64_t full = n / (2 * b);  // pairs with both blocks complete
+    const int64_t stride = 2 * b * (n + 1);
+    if (full > 0) {
+      if (use_oz(b, b, b)) {
+        for (int64_t i = 0; i < full; ++i) {
+          const int64_t a0 = 2 * b * i, b0 = a0 + b;
+          TNX_TRY(gemm_fp64_class_oz(true, false, false, b, b, b, 1.0, y.S + a0 * n + b0, n, y.Tf + b0 * n + b0, n,
+                                     0.0, y.Y, b, y.oz, y.oz_bytes, st));
+          TNX_TRY(gemm_fp64_class_oz(true, false, false, b, b, b, -1.0, y.Tf + a0 * n + a0, n, y.Y, b, 0.0,
+                                     y.Tf + a0 * n + b0, n, y.oz, y.oz_bytes, st));
+        }
+      } else {
+        TNX_TRY(gemm_fp64_class(true, false, false, b, b, b, 1.0, y.S + b, n, stride, y.Tf + b * n + b, n, stride, 0.0,
+                                y.Y, b, b * b, full, st));
+        TNX_TRY(gemm_fp64_class(true, false, false, b, b, b, -1.0, y.Tf, n, stride, y.Y, b, b * b, 0.0, y.Tf + b, n,
+                                stride, full, st));
+      }
+    }
+    const int64_t a0 = 2 * b * full, b0 = a0 + b;
+    if (b0 < n) {  // trailing pair with a short B block
+      const int64_t nbB = n - b0;
+      TNX_TRY(gemm_fp64_class(true, false, false, b, nbB, nbB, 1.0, y.S + a0 * n + b0, n, 0, y.Tf + b0 * n + b0, n,
+                              0, 0.0, y.Y, nbB, 0, 1, st));
+      TNX_TRY(gemm_fp64_class(true, false, false, b, nbB, b, -1.0, y.Tf + a0 * n + a0, n, 0, y.Y, nbB, 0, 0.0,
+                              y.Tf + a0 * n + b0, n, 0, 1, st));
+    }
+  }
+  // X = Tf V_top^T  (op(B)(k, j) = V(j, k) = V[k m + j])
+  TNX_TRY(gemm_fp64_class_oz(true, false, false, n, n, n, 1.0, y.Tf, n, y.V, m, 0.0, y.X, n, y.oz, y.oz_bytes, st));
+  if (q_rowmajor) {
+    // Q = [I; 0] - V X  (op(A)(i, k) = V(i, k) = V[k m + i])
+    eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(Q, n, m);
+    TNX_LAUNCH_CHECK();
+    TNX_TRY(gemm_fp64_class_oz(true, true, false, m, n, n, -1.0, y.V, m, y.X, n, 1.0, Q, n, y.oz, y.oz_bytes, st));
+  } else {
+    // Q^T = [I, 0] - X^T V^T  (row-major n x m)
+    eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(Q, m, n);
+    TNX_LAUNCH_CHECK();
+    TNX_TRY(gemm_fp64_class_oz(true, true, false, n, m, n, -1.0, y.X, n, y.V, m, 1.0, Q, m, y.oz, y.oz_bytes, st));
   }
   return TNX_OK;
 }
@@ -782,7 +1024,8 @@ size_t tnx_gauge_move_workspace_bytes(int direction, int64_t chi_l, int64_t d, i
   int64_t n = direction == 1 ? chi_r : chi_l;
   int64_t nb_elems = direction == 1 ? chi_r * d * chi_other : chi_other * d * chi_l;
   return qr_layout(m, n, nullptr, nullptr) + align_up(n * n * 8) + align_up(nb_elems * 8) +
-         align_up(gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other));
+         align_up(gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other)) +
+         (wy_applies(m, n, true) ? wy_layout(m, n, nullptr, nullptr) : 0);
 }
 
 int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, int64_t d, int64_t chi_r,
@@ -807,16 +1050,26 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
   double* tmp = reinterpret_cast<double*>(static_cast<char*>(workspace) + qbytes + align_up(n * n * 8));
   const int64_t nb_elems = direction == 1 ? chi_r * d * chi_other : chi_other * d * chi_l;
   const size_t ozb = df ? gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other) : 0;
-  void* oz = ozb ? static_cast<void*>(reinterpret_cast<char*>(tmp) + align_up(nb_elems * 8)) : nullptr;
+  char* after_tmp = reinterpret_cast<char*>(tmp) + align_up(nb_elems * 8);
+  void* oz = ozb ? static_cast<void*>(after_tmp) : nullptr;
+  // Q from the compact WY form on the tensor cores (FP64-class modes, large bonds)
+  const bool wy = wy_applies(m, n, df);
+  WyWs wys{};
+  if (wy) wy_layout(m, n, after_tmp + align_up(gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other)), &wys);
+  const int NB = plan_panels(m, df).nb;
   cudaStream_t st = as_stream(stream);
   dim3 tb(32, 8);
   if (direction == 1) {
     // psi (chi_l d x chi_r) row-major -> column-major
     transpose_kernel<<<dim3(unsigned((n + 31) / 32), unsigned((m + 31) / 32)), tb, 0, st>>>(A_site, m, n, w.F);
     TNX_LAUNCH_CHECK();
-    TNX_TRY(qr_colmajor(m, n, w, st, df));
-    transpose_kernel<<<dim3(unsigned((m + 31) / 32), unsigned((n + 31) / 32)), tb, 0, st>>>(w.Qc, n, m, A_site);
-    TNX_LAUNCH_CHECK();
+    TNX_TRY(qr_colmajor(m, n, w, st, df, !wy));
+    if (wy) {
+      TNX_TRY(form_q_wy(m, n, NB, w, wys, A_site, true, st));
+    } else {
+      transpose_kernel<<<dim3(unsigned((m + 31) / 32), unsigned((n + 31) / 32)), tb, 0, st>>>(w.Qc, n, m, A_site);
+      TNX_LAUNCH_CHECK();
+    }
     extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
     TNX_LAUNCH_CHECK();
     // A_next (chi_r x d chi_other) <- R A_next
@@ -826,9 +1079,13 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
   } else {
     // psi (chi_l x d chi_r) row-major == psi^T (d chi_r x chi_l) column-major
     TNX_CUDA(cudaMemcpyAsync(w.F, A_site, m * n * 8, cudaMemcpyDeviceToDevice, st));
-    TNX_TRY(qr_colmajor(m, n, w, st, df));
+    TNX_TRY(qr_colmajor(m, n, w, st, df, !wy));
     // Q column-major (d chi_r x chi_l) == Q^T row-major (chi_l x d chi_r)
-    TNX_CUDA(cudaMemcpyAsync(A_site, w.Qc, m * n * 8, cudaMemcpyDeviceToDevice, st));
+    if (wy) {
+      TNX_TRY(form_q_wy(m, n, NB, w, wys, A_site, false, st));
+    } else {
+      TNX_CUDA(cudaMemcpyAsync(A_site, w.Qc, m * n * 8, cudaMemcpyDeviceToDevice, st));
+    }
     extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
     TNX_LAUNCH_CHECK();
     // A_prev (chi_other d x chi_l) <- A_prev R^T

@@ -13,7 +13,9 @@
 //   * 512 threads, 8 per panel column interleaved over rows, two independent accumulators,
 //     (hi, lo) pairs interleaved in shared memory;
 //     dot products accumulate compensated (hi, lo) sums renormalised once at the end;
-//   * the CL partial sums of a column are added as a fixed binary tree (every CTA derives
+//   * every CTA pushes its partial sums into every CTA's shared memory (remote stores before
+//     the cluster barrier), so the gather after the barrier reads only local shared memory;
+//     the CL partial sums of a column are added as a fixed binary tree (every CTA derives
 //     bitwise-identical column scalars);
 //   * the column scalars use 1 / norm from an rsqrtf seed refined by Newton steps in
 //     double-FP32 (tau = 1 + |alpha| / norm needs no division; scale = sign / (norm tau) one
@@ -154,17 +156,26 @@ __device__ __forceinline__ void cluster_wait_acquire() {
   asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory");
 }
 
-// Sum of the CL partials slot(rank)[idx] over the cluster, as a fixed binary tree
+// Sum of the CL partials recv[rank * stride + idx] (pushed by every CTA of the cluster into
+// this CTA's shared memory), as a fixed binary tree: every CTA derives the same bits
 template <int CL>
-__device__ __forceinline__ df2 tree_sum(cg::cluster_group& cluster, const df2* slot, int idx) {
+__device__ __forceinline__ df2 tree_sum(const df2* recv, int stride, int idx) {
   df2 v[CL];
 #pragma unroll
-  for (int r = 0; r < CL; ++r) v[r] = cluster.map_shared_rank(slot, r)[idx];
+  for (int r = 0; r < CL; ++r) v[r] = recv[r * stride + idx];
 #pragma unroll
   for (int s = 1; s < CL; s <<= 1)
 #pragma unroll
     for (int r = 0; r + s < CL; r += 2 * s) v[r] = add(v[r], v[r + s]);
   return v[0];
+}
+
+// Store v at the same shared-memory location in every CTA of the cluster (distributed shared
+// memory); the next cluster barrier (arrive.release / wait.acquire) makes the stores visible
+template <int CL>
+__device__ __forceinline__ void push_all(cg::cluster_group& cluster, df2* local, df2 v) {
+#pragma unroll
+  for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(local, r) = v;
 }
 
 // Dynamic shared memory bytes of one CTA: (hi, lo) pairs of the panel [NB][ld], of v and of
@@ -196,7 +207,11 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
   df2* X = pd;                        // [NB][ld] panel rows of this CTA, column-major
   df2* V = pd + NB * ld;              // reflector of the current column over this CTA's rows
   df2* N = V + ld;                    // next column after the current reflector
-  __shared__ df2 slot[2][3][NB];      // exchange: partial dots, pivot row, partial T dots
+  // exchange, double-buffered by column parity and pushed by every CTA into every CTA's copy:
+  // partial dots per source rank (kind 0: dots / norm of the next column, kind 1: T dots) and
+  // the pivot row (from its owner)
+  __shared__ df2 rsum[2][2][CL][NB];
+  __shared__ df2 rpiv[2][NB];
   __shared__ unsigned long long smax[NB];
   __shared__ df2 S[NB], P[NB], Z[NB], taus[NB], sc[4];
   __shared__ df2 Tr[NR][NB];          // rows q, q + CL, ... of T
@@ -258,8 +273,8 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
 #pragma unroll
     for (int o = TPC / 2; o > 0; o >>= 1) a0 = add(a0, shfl_xor(a0, o));
     if (ci < nb && h == 0) {
-      slot[0][0][ci] = a0;
-      if (r0 == 0 && rows > 0) slot[0][1][ci] = X[ci * ld];
+      push_all<CL>(cluster, &rsum[0][0][q][ci], a0);
+      if (r0 == 0 && rows > 0) push_all<CL>(cluster, &rpiv[0][ci], X[ci * ld]);
     }
   }
   cluster_arrive_release();
@@ -272,17 +287,16 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
 #endif
     PANEL_STAMP(0);
     const int par = jj & 1;
-    const int owner = int(jj / rpc);
     // ---- gather: S[c] (c >= jj), pivot row P[c], T dots Z[a] = v_a . v_{jj-1} (a < jj - 1)
     if (tid < NB) {
       const int c = tid;
       if (c >= jj && c < nb) {
-        S[c] = tree_sum<CL>(cluster, &slot[par][0][0], c);
-        P[c] = cluster.map_shared_rank(&slot[par][1][0], owner)[c];
+        S[c] = tree_sum<CL>(&rsum[par][0][0][0], NB, c);
+        P[c] = rpiv[par][c];
       }
     } else if (tid < 2 * NB) {
       const int a = tid - NB;
-      if (a < jj - 1) Z[a] = tree_sum<CL>(cluster, &slot[par][2][0], a);
+      if (a < jj - 1) Z[a] = tree_sum<CL>(&rsum[par][1][0][0], NB, a);
     }
     __syncthreads();
     PANEL_STAMP(1);
@@ -330,7 +344,6 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
     const bool own_ln = ln >= 0 && ln < rows && int(ln % TPC) == h;
     const int rB = int(lj + 2 > 0 ? lj + 2 : 0);
     const int rB0 = rB + ((h - rB) % TPC + TPC) % TPC;  // first row >= rB held by this thread
-    df2(*nxt)[NB] = slot[par ^ 1];
     if (ci < nb && ci > jj + 1) {
       df2* xc = X + ci * ld;
       const df2 wc = mul(tj, add(P[ci], mul(scale, S[ci])));
@@ -338,7 +351,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
       if (own_ln) {
         const df2 t = fms(xc[ln], wc, V[ln]);
         xc[ln] = t;
-        nxt[1][ci] = t;
+        push_all<CL>(cluster, &rpiv[par ^ 1][ci], t);
       }
       int r = rB0;
       for (; r + TPC < rows; r += 2 * TPC) {
@@ -355,7 +368,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
         acc(a0, N[r], t0);
       }
     } else if (ci == jj + 1 && ci < nb) {
-      if (own_ln) nxt[1][ci] = N[ln];
+      if (own_ln) push_all<CL>(cluster, &rpiv[par ^ 1][ci], N[ln]);
       int r = rB0;
       for (; r + TPC < rows; r += 2 * TPC) {
         acc(a0, N[r], N[r]);
@@ -375,8 +388,8 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
 #pragma unroll
     for (int o = TPC / 2; o > 0; o >>= 1) a = add(a, shfl_xor(a, o));
     if (h == 0 && ci < nb) {
-      if (ci > jj) nxt[0][ci] = a;
-      else if (ci < jj) nxt[2][ci] = a;
+      if (ci > jj) push_all<CL>(cluster, &rsum[par ^ 1][0][q][ci], a);
+      else if (ci < jj) push_all<CL>(cluster, &rsum[par ^ 1][1][q][ci], a);
     }
     PANEL_STAMP(4);
     cluster_arrive_release();
@@ -412,7 +425,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
   // last T column k = nb - 1 from the final exchange
   if (tid >= NB && tid < 2 * NB) {
     const int a = tid - NB;
-    if (a < nb - 1) Z[a] = tree_sum<CL>(cluster, &slot[nb & 1][2][0], a);
+    if (a < nb - 1) Z[a] = tree_sum<CL>(&rsum[nb & 1][1][0][0], NB, a);
   }
   __syncthreads();
   {
@@ -445,7 +458,8 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
     const df2 v = X[c * ld + r];
     F[(j0 + c) * m + j0 + r0 + r] = r0 + r <= c ? join_scaled(v, cexp[c]) : join_df(v.h, v.l);
   }
-  // no CTA leaves while another may still read its slots
+  // every push into another CTA's shared memory precedes the last barrier of the loop; this one
+  // keeps the CTAs' exits ordered after it all the same
   cluster_arrive_release();
   cluster_wait_acquire();
 }

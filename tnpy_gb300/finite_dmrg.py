@@ -328,18 +328,7 @@ class ShiftInvertDMRG(FiniteDMRG):
         x = self.mps.tensors[site]
         if x.numel() < self._exact_solver_dim:
             self.stats["dense_solves"] += 1
-            a = self._env.one_site_full_matrix(site)
-            b = self._env2.one_site_full_matrix(site)
-            n = a.shape[0]
-            wb, ub = K.eigh_batched([(0.5 * (b + b.T)).contiguous()], keep=n)
-            ub = ub[0, :n, :]
-            if float(wb.min().item()) <= 0.0:
-                raise RuntimeError(f"site {site}: the squared operator is not positive definite")
-            bih = K.gemm((ub * wb[0].rsqrt()[None, :]).contiguous(), ub, trans_b=True)  # B^-1/2
-            c = K.gemm(bih, K.gemm(a, bih))
-            wc, uc = K.eigh_batched([(0.5 * (c + c.T)).contiguous()], keep=1)
-            vec = K.gemm(bih, uc[0, :n, :].contiguous())
-            return float(wc[0, 0].item()), vec.reshape(x.shape).contiguous()
+            return self._dense_solve(site, x)
         self.stats["iterative_solves"] += 1
         psi = x.clone()
         L, W, R = self._env.site_operator(site)
@@ -349,9 +338,45 @@ class ShiftInvertDMRG(FiniteDMRG):
                                       max_basis=kwargs.get("max_basis", self.max_basis), precision=self.precision)
         self.stats["matvecs"] += its
         if not ok:
+            if x.numel() <= self.DENSE_FALLBACK_DIM:
+                # pencils with an ill-conditioned B can stall the Davidson far from its target:
+                # solve such a site densely instead
+                self.stats["dense_fallbacks"] = self.stats.get("dense_fallbacks", 0) + 1
+                logger.info(f"site {site}: generalised Davidson stalled (residual {rn:.3e}); dense solve")
+                return self._dense_solve(site, x)
             self.stats["unconverged"] += 1
             logger.warning(f"site {site}: generalised Davidson did not converge (residual {rn:.3e}, {its} expansions)")
         return e, psi
+
+    DENSE_FALLBACK_DIM = 4096
+
+    def _dense_solve(self, site: int, x: torch.Tensor):
+        """Smallest eigenpair of the dense pencil: B^-1/2 A B^-1/2 (B^-1/2 from the eigenpairs of
+        B) and its lowest eigenvector mapped back, as scipy.linalg.eigh(a, b) does by Cholesky."""
+        from .exact_diagonalization import eigh_full
+
+        a = self._env.one_site_full_matrix(site)
+        b = self._env2.one_site_full_matrix(site)
+        n = a.shape[0]
+        sym = lambda m: (0.5 * (m + m.T)).contiguous()
+        if n < 200:
+            wb, ub = K.eigh_batched([sym(b)], keep=n)
+            wb, ub = wb[0], ub[0, :n, :]
+        else:
+            wbh, ub = eigh_full(sym(b))
+            wb = torch.as_tensor(wbh.copy(), device=b.device)
+        if float(wb.min().item()) <= 0.0:
+            raise RuntimeError(f"site {site}: the squared operator is not positive definite")
+        bih = K.gemm((ub * wb.rsqrt()[None, :]).contiguous(), ub, trans_b=True)  # B^-1/2
+        c = K.gemm(bih, K.gemm(a, bih))
+        if n < 200:
+            wc, uc = K.eigh_batched([sym(c)], keep=1)
+            lam, u0 = float(wc[0, 0].item()), uc[0, :n, :1]
+        else:
+            wch, uc = eigh_full(sym(c))
+            lam, u0 = float(wch[0]), uc[:, :1]
+        vec = K.gemm(bih, u0.contiguous())
+        return lam, vec.reshape(x.shape).contiguous()
 
     def sweep(self, direction: Direction = Direction.RIGHTWARD, tol: float = 1e-8, **kwargs) -> float | None:
         """:365-384: the FiniteDMRG site update, plus the MPO-square environments."""
