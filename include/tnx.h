@@ -237,7 +237,9 @@ int tnx_batched_env_update(int direction, const double* E_in, int64_t sE, const 
  * basis) and every vector kernel skips it from then on. X: in = start vectors, out = unit Ritz
  * vectors. evals_out / resid_out (device, batch doubles), active_out (device, batch ints, may
  * be null): 1 for chains still unconverged after max_iter expansions (TNX_ERR_NOT_CONVERGED),
- * *iters_out = expansions run. One host read (the active count) every fourth expansion; restarts
+ * *iters_out = expansions run. Once at most batch / 64 chains are still active, those get as many
+ * more expansions as the batch had taken by then (at least 32) and stop with their current Ritz
+ * pair, reported unconverged. One host read (the active count) every fourth expansion; restarts
  * keep two vectors per chain (the Ritz vector and the previous one, GD+1), and the products of
  * retired chains are skipped. */
 size_t tnx_batched_davidson1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,

@@ -664,6 +664,13 @@ int tnx_batched_davidson1(const double* L, int64_t sL, const double* W, int64_t 
   bcopy_kernel<<<dim3(vchunks, B), BT, 0, st>>>(X, sX, w.t, n, n, nullptr);
   TNX_LAUNCH_CHECK();
   int k = 0, iters = 0, host_count = B;
+  // Stragglers: once at most B / 64 chains are still active (it_most: the expansion at which
+  // that was first seen), the remaining chains get max(it_most, 32) more expansions and then
+  // stop with their current Ritz pair (reported as not converged). Every expansion of a
+  // lockstep batch costs the launches of the whole batch, so one slow chain at 400 expansions
+  // would otherwise cost as much as the rest of the site.
+  const int straggler_max = B / 64;
+  int it_most = -1;
   for (;;) {
     double* vk = w.V + int64_t(k) * n;
     bcopy_kernel<<<dim3(vchunks, B), BT, 0, st>>>(w.t, n, vk, sVB, n, w.active);
@@ -705,6 +712,8 @@ int tnx_batched_davidson1(const double* L, int64_t sL, const double* W, int64_t 
       TNX_CUDA(cudaMemcpyAsync(&host_count, w.count, sizeof(int), cudaMemcpyDeviceToHost, st));
       TNX_CUDA(cudaStreamSynchronize(st));
       if (host_count == 0 || iters >= max_iter || k >= n) break;
+      if (it_most < 0 && host_count <= straggler_max) it_most = iters;
+      if (it_most >= 0 && iters >= it_most + (it_most > 32 ? it_most : 32)) break;
     }
     if (k == mb) {  // GD+1 restart of every active chain: its Ritz vector and the previous one
       brestart_plus_kernel<<<B, BT, 0, st>>>(w.V, w.AV, sVB, n, k, w.Hm, int64_t(mb) * mb, mb, w.evecs,

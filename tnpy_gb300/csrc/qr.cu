@@ -645,7 +645,7 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
 // between two panels. As three general GEMM launches (split-K V^T C with its reduction, T^T W,
 // C -= V W) it is latency-bound at 64 x 64 x (m - j0); these kernels spread each phase over
 // all rows of the GPU instead: NR_ROWS-row chunks of V^T C per CTA, a fixed-order reduction of
-// the chunk partials fused with T^T W, and the rank-nb update per row chunk.
+// the chunk partials, T^T W, and the rank-nb update per row chunk.
 constexpr int NR_ROWS = 16;   // rows of V and C per CTA in the partial and update kernels
 constexpr int NR_T = 256;     // threads of those kernels
 
@@ -683,18 +683,34 @@ __global__ void __launch_bounds__(NR_T) nar_partial_kernel(const double* __restr
   for (int j = 0; j < 16; ++j) out[a * 64 + bq + 4 * j] = qrdf::norm(acc[j]);
 }
 
-// W2[a][b] = sum_k T(k, a) W[k][b], W[k][b] = sum over chunks of part[c][k][b] in chunk order;
-// one CTA of 64 threads per column b; T column-major (ld NB), upper triangular
-__global__ void __launch_bounds__(64) nar_reduce_kernel(const qrdf::df2* __restrict__ part, int nchunk, int nb,
-                                                        const double* __restrict__ T, int NB,
-                                                        qrdf::df2* __restrict__ W2) {
-  __shared__ qrdf::df2 Ws[64];
-  const int b = blockIdx.x, k = threadIdx.x;
+// W[o] = sum over chunks c of part[c][o] in chunk order, o = k * 64 + b (threads over o:
+// coalesced, four independent loads in flight)
+__global__ void __launch_bounds__(256) nar_reduce_kernel(const qrdf::df2* __restrict__ part, int nchunk,
+                                                         qrdf::df2* __restrict__ W) {
+  const int o = blockIdx.x * 256 + threadIdx.x;
   qrdf::df2 s = {0.f, 0.f};
-  for (int c = 0; c < nchunk; ++c) s = qrdf::add(s, part[int64_t(c) * 64 * 64 + k * 64 + b]);
-  Ws[k] = s;
+  int c = 0;
+  for (; c + 4 <= nchunk; c += 4) {
+    const qrdf::df2 p0 = part[int64_t(c) * 4096 + o], p1 = part[int64_t(c + 1) * 4096 + o],
+                    p2 = part[int64_t(c + 2) * 4096 + o], p3 = part[int64_t(c + 3) * 4096 + o];
+    s = qrdf::add(s, p0);
+    s = qrdf::add(s, p1);
+    s = qrdf::add(s, p2);
+    s = qrdf::add(s, p3);
+  }
+  for (; c < nchunk; ++c) s = qrdf::add(s, part[int64_t(c) * 4096 + o]);
+  W[o] = s;
+}
+
+// W2[a][b] = sum_{k <= a} T(k, a) W[k][b]; one CTA of 64 threads per column b, T column-major
+// (ld NB), upper triangular
+__global__ void __launch_bounds__(64) nar_tmul_kernel(const qrdf::df2* __restrict__ W, int nb,
+                                                      const double* __restrict__ T, int NB,
+                                                      qrdf::df2* __restrict__ W2) {
+  __shared__ qrdf::df2 Ws[64];
+  const int b = blockIdx.x, a = threadIdx.x;
+  Ws[a] = W[a * 64 + b];
   __syncthreads();
-  const int a = threadIdx.x;
   qrdf::df2 t = {0.f, 0.f};
   if (a < nb)
     for (int kk = 0; kk <= a; ++kk) {
@@ -743,14 +759,16 @@ __global__ void __launch_bounds__(NR_T) nar_update_kernel(const double* __restri
 }
 
 // C -= V T^T V^T C for a block of nc <= 64 columns (the next panel), double-FP32 arithmetic;
-// part holds ceil(mp / NR_ROWS) * 64 * 64 float pairs, W2 64 * 64
+// part holds ceil(mp / NR_ROWS) * 64 * 64 float pairs, W and W2 64 * 64 each
 int apply_panel_narrow(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int nc,
-                       qrdf::df2* W2, qrdf::df2* part, cudaStream_t st) {
+                       qrdf::df2* W, qrdf::df2* W2, qrdf::df2* part, cudaStream_t st) {
   const int nchunk = int((mp + NR_ROWS - 1) / NR_ROWS);
   profile_mark(KF_F64_GEMM, st, true);
   nar_partial_kernel<<<nchunk, NR_T, 0, st>>>(Vp, mp, nb, C, m, nc, part);
   TNX_LAUNCH_CHECK();
-  nar_reduce_kernel<<<nc, 64, 0, st>>>(part, nchunk, nb, Tp, NB, W2);
+  nar_reduce_kernel<<<16, 256, 0, st>>>(part, nchunk, W);
+  TNX_LAUNCH_CHECK();
+  nar_tmul_kernel<<<nc, 64, 0, st>>>(W, nb, Tp, NB, W2);
   TNX_LAUNCH_CHECK();
   nar_update_kernel<<<nchunk, NR_T, 0, st>>>(Vp, mp, nb, W2, C, m, nc);
   TNX_LAUNCH_CHECK();
@@ -839,8 +857,8 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
     }
     const bool narrow = df && n >= 64 && (mp + NR_ROWS - 1) / NR_ROWS * 64 * 64 <= part_cap;
     if (narrow) {
-      TNX_TRY(apply_panel_narrow(m, mp, nb, NB, Vp, Tp, Cn, nb1, reinterpret_cast<qrdf::df2*>(w.W2),
-                                 reinterpret_cast<qrdf::df2*>(w.part), st));
+      TNX_TRY(apply_panel_narrow(m, mp, nb, NB, Vp, Tp, Cn, nb1, reinterpret_cast<qrdf::df2*>(w.W1),
+                                 reinterpret_cast<qrdf::df2*>(w.W2), reinterpret_cast<qrdf::df2*>(w.part), st));
     } else {
       TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, st, df));
     }

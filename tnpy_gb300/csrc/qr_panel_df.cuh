@@ -13,9 +13,7 @@
 //   * 512 threads, 8 per panel column interleaved over rows, two independent accumulators,
 //     (hi, lo) pairs interleaved in shared memory;
 //     dot products accumulate compensated (hi, lo) sums renormalised once at the end;
-//   * every CTA pushes its partial sums into every CTA's shared memory (remote stores before
-//     the cluster barrier), so the gather after the barrier reads only local shared memory;
-//     the CL partial sums of a column are added as a fixed binary tree (every CTA derives
+//   * the CL partial sums of a column are added as a fixed binary tree (every CTA derives
 //     bitwise-identical column scalars);
 //   * the column scalars use 1 / norm from an rsqrtf seed refined by Newton steps in
 //     double-FP32 (tau = 1 + |alpha| / norm needs no division; scale = sign / (norm tau) one
@@ -156,26 +154,17 @@ __device__ __forceinline__ void cluster_wait_acquire() {
   asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory");
 }
 
-// Sum of the CL partials recv[rank * stride + idx] (pushed by every CTA of the cluster into
-// this CTA's shared memory), as a fixed binary tree: every CTA derives the same bits
+// Sum of the CL partials slot(rank)[idx] over the cluster, as a fixed binary tree
 template <int CL>
-__device__ __forceinline__ df2 tree_sum(const df2* recv, int stride, int idx) {
+__device__ __forceinline__ df2 tree_sum(cg::cluster_group& cluster, const df2* slot, int idx) {
   df2 v[CL];
 #pragma unroll
-  for (int r = 0; r < CL; ++r) v[r] = recv[r * stride + idx];
+  for (int r = 0; r < CL; ++r) v[r] = cluster.map_shared_rank(slot, r)[idx];
 #pragma unroll
   for (int s = 1; s < CL; s <<= 1)
 #pragma unroll
     for (int r = 0; r + s < CL; r += 2 * s) v[r] = add(v[r], v[r + s]);
   return v[0];
-}
-
-// Store v at the same shared-memory location in every CTA of the cluster (distributed shared
-// memory); the next cluster barrier (arrive.release / wait.acquire) makes the stores visible
-template <int CL>
-__device__ __forceinline__ void push_all(cg::cluster_group& cluster, df2* local, df2 v) {
-#pragma unroll
-  for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(local, r) = v;
 }
 
 // Dynamic shared memory bytes of one CTA: (hi, lo) pairs of the panel [NB][ld], of v and of
@@ -207,11 +196,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
   df2* X = pd;                        // [NB][ld] panel rows of this CTA, column-major
   df2* V = pd + NB * ld;              // reflector of the current column over this CTA's rows
   df2* N = V + ld;                    // next column after the current reflector
-  // exchange, double-buffered by column parity and pushed by every CTA into every CTA's copy:
-  // partial dots per source rank (kind 0: dots / norm of the next column, kind 1: T dots) and
-  // the pivot row (from its owner)
-  __shared__ df2 rsum[2][2][CL][NB];
-  __shared__ df2 rpiv[2][NB];
+  __shared__ df2 slot[2][3][NB];      // exchange: partial dots, pivot row, partial T dots
   __shared__ unsigned long long smax[NB];
   __shared__ df2 S[NB], P[NB], Z[NB], taus[NB], sc[4];
   __shared__ df2 Tr[NR][NB];          // rows q, q + CL, ... of T
@@ -273,8 +258,8 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
 #pragma unroll
     for (int o = TPC / 2; o > 0; o >>= 1) a0 = add(a0, shfl_xor(a0, o));
     if (ci < nb && h == 0) {
-      push_all<CL>(cluster, &rsum[0][0][q][ci], a0);
-      if (r0 == 0 && rows > 0) push_all<CL>(cluster, &rpiv[0][ci], X[ci * ld]);
+      slot[0][0][ci] = a0;
+      if (r0 == 0 && rows > 0) slot[0][1][ci] = X[ci * ld];
     }
   }
   cluster_arrive_release();
@@ -287,16 +272,17 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
 #endif
     PANEL_STAMP(0);
     const int par = jj & 1;
+    const int owner = int(jj / rpc);
     // ---- gather: S[c] (c >= jj), pivot row P[c], T dots Z[a] = v_a . v_{jj-1} (a < jj - 1)
     if (tid < NB) {
       const int c = tid;
       if (c >= jj && c < nb) {
-        S[c] = tree_sum<CL>(&rsum[par][0][0][0], NB, c);
-        P[c] = rpiv[par][c];
+        S[c] = tree_sum<CL>(cluster, &slot[par][0][0], c);
+        P[c] = cluster.map_shared_rank(&slot[par][1][0], owner)[c];
       }
     } else if (tid < 2 * NB) {
       const int a = tid - NB;
-      if (a < jj - 1) Z[a] = tree_sum<CL>(&rsum[par][1][0][0], NB, a);
+      if (a < jj - 1) Z[a] = tree_sum<CL>(cluster, &slot[par][2][0], a);
     }
     __syncthreads();
     PANEL_STAMP(1);
@@ -344,6 +330,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
     const bool own_ln = ln >= 0 && ln < rows && int(ln % TPC) == h;
     const int rB = int(lj + 2 > 0 ? lj + 2 : 0);
     const int rB0 = rB + ((h - rB) % TPC + TPC) % TPC;  // first row >= rB held by this thread
+    df2(*nxt)[NB] = slot[par ^ 1];
     if (ci < nb && ci > jj + 1) {
       df2* xc = X + ci * ld;
       const df2 wc = mul(tj, add(P[ci], mul(scale, S[ci])));
@@ -351,7 +338,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
       if (own_ln) {
         const df2 t = fms(xc[ln], wc, V[ln]);
         xc[ln] = t;
-        push_all<CL>(cluster, &rpiv[par ^ 1][ci], t);
+        nxt[1][ci] = t;
       }
       int r = rB0;
       for (; r + TPC < rows; r += 2 * TPC) {
@@ -368,7 +355,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
         acc(a0, N[r], t0);
       }
     } else if (ci == jj + 1 && ci < nb) {
-      if (own_ln) push_all<CL>(cluster, &rpiv[par ^ 1][ci], N[ln]);
+      if (own_ln) nxt[1][ci] = N[ln];
       int r = rB0;
       for (; r + TPC < rows; r += 2 * TPC) {
         acc(a0, N[r], N[r]);
@@ -388,8 +375,8 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
 #pragma unroll
     for (int o = TPC / 2; o > 0; o >>= 1) a = add(a, shfl_xor(a, o));
     if (h == 0 && ci < nb) {
-      if (ci > jj) push_all<CL>(cluster, &rsum[par ^ 1][0][q][ci], a);
-      else if (ci < jj) push_all<CL>(cluster, &rsum[par ^ 1][1][q][ci], a);
+      if (ci > jj) nxt[0][ci] = a;
+      else if (ci < jj) nxt[2][ci] = a;
     }
     PANEL_STAMP(4);
     cluster_arrive_release();
@@ -425,7 +412,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
   // last T column k = nb - 1 from the final exchange
   if (tid >= NB && tid < 2 * NB) {
     const int a = tid - NB;
-    if (a < nb - 1) Z[a] = tree_sum<CL>(&rsum[nb & 1][1][0][0], NB, a);
+    if (a < nb - 1) Z[a] = tree_sum<CL>(cluster, &slot[nb & 1][2][0], a);
   }
   __syncthreads();
   {
@@ -458,8 +445,7 @@ __global__ void __launch_bounds__(DPT) panel_df_kernel(double* __restrict__ F, i
     const df2 v = X[c * ld + r];
     F[(j0 + c) * m + j0 + r0 + r] = r0 + r <= c ? join_scaled(v, cexp[c]) : join_df(v.h, v.l);
   }
-  // every push into another CTA's shared memory precedes the last barrier of the loop; this one
-  // keeps the CTAs' exits ordered after it all the same
+  // no CTA leaves while another may still read its slots
   cluster_arrive_release();
   cluster_wait_acquire();
 }

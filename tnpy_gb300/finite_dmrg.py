@@ -424,7 +424,9 @@ class BatchedFiniteDMRG:
     seeds: ``seed + c``) exactly as ``FiniteDMRG(mpos[c], bond_dim, seed=seeds[c])`` does, and
     each site update applies the reference's steps to every chain at once: the lowest eigenpair
     (dense Jacobi below ``exact_solver_dim`` elements, else the batched Davidson with a per-chain
-    convergence mask), the 1e-5 perturbation, the QR gauge move and the environment update. A
+    convergence mask; in batches of 64 chains or more, the last <= 1/64 of the chains stop after
+    twice the expansions the rest needed and keep their best Ritz vector, counted in
+    ``stats['unconverged']``), the 1e-5 perturbation, the QR gauge move and the environment update. A
     chain stops recording energies once its |dE| < tol (its ``energies`` end there, as in
     FiniteDMRG.run); the batch sweeps until every chain has converged or max_sweep.
 
