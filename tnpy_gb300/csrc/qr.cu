@@ -645,17 +645,18 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
 // between two panels. As three general GEMM launches (split-K V^T C with its reduction, T^T W,
 // C -= V W) it is latency-bound at 64 x 64 x (m - j0); these kernels spread each phase over
 // all rows of the GPU instead: NR_ROWS-row chunks of V^T C per CTA, a fixed-order reduction of
-// the chunk partials, T^T W, and the rank-nb update per row chunk.
+// the chunk partials fused with T^T W, and the rank-nb update per row chunk.
 constexpr int NR_ROWS = 16;   // rows of V and C per CTA in the partial and update kernels
 constexpr int NR_T = 256;     // threads of those kernels
 
-// part[c][a][b] = sum over rows r of chunk c of V[r][a] C[r][b]  (a < nb, b < nc <= 64; df2)
+// part[c][b][a] = sum over rows r of chunk c of V[r][a] C[r][b]  (a < nb, b < nc <= 64; df2)
 __global__ void __launch_bounds__(NR_T) nar_partial_kernel(const double* __restrict__ Vp, int64_t mp, int nb,
                                                            const double* __restrict__ C, int64_t ldc, int nc,
                                                            qrdf::df2* __restrict__ part) {
   __shared__ qrdf::df2 Vs[NR_ROWS][64], Cs[NR_ROWS][64];
   const int tid = threadIdx.x;
   const int64_t r0 = int64_t(blockIdx.x) * NR_ROWS;
+#pragma unroll
   for (int e = tid; e < NR_ROWS * 64; e += NR_T) {
     const int r = e % NR_ROWS, c = e / NR_ROWS;
     const int64_t gr = r0 + r;
@@ -680,45 +681,54 @@ __global__ void __launch_bounds__(NR_T) nar_partial_kernel(const double* __restr
   }
   qrdf::df2* out = part + int64_t(blockIdx.x) * 64 * 64;
 #pragma unroll
-  for (int j = 0; j < 16; ++j) out[a * 64 + bq + 4 * j] = qrdf::norm(acc[j]);
+  for (int j = 0; j < 16; ++j) out[(bq + 4 * j) * 64 + a] = qrdf::norm(acc[j]);
 }
 
-// W[o] = sum over chunks c of part[c][o] in chunk order, o = k * 64 + b (threads over o:
-// coalesced, four independent loads in flight)
-__global__ void __launch_bounds__(256) nar_reduce_kernel(const qrdf::df2* __restrict__ part, int nchunk,
-                                                         qrdf::df2* __restrict__ W) {
-  const int o = blockIdx.x * 256 + threadIdx.x;
+// W2[a][b] = sum_{k <= a} T(k, a) W[k][b] with W[k][b] = sum over chunks c of part[c][b][k]; one
+// CTA of 256 threads per column b: thread (g, k) sums the chunks c = g (mod 4) in order
+// (coalesced loads, four in flight), the four group sums are added in group order, and T
+// (column-major, ld NB, upper triangular) is staged in shared memory by all threads at once
+constexpr int NRED_T = 256;
+__global__ void __launch_bounds__(NRED_T) nar_reduce_kernel(const qrdf::df2* __restrict__ part, int nchunk, int nb,
+                                                            const double* __restrict__ T, int NB,
+                                                            qrdf::df2* __restrict__ W2) {
+  __shared__ qrdf::df2 Wg[4][64];
+  __shared__ double Ts[64][65];
+  const int b = blockIdx.x, tid = threadIdx.x, k = tid & 63, g = tid >> 6;
+#pragma unroll
+  for (int i = 0; i < 64 * 64 / NRED_T; ++i) {
+    const int e = tid + i * NRED_T, col = e / 64, row = e % 64;  // T(row, col)
+    Ts[col][row] = (row < nb && col < nb) ? T[col * NB + row] : 0.0;
+  }
+  const qrdf::df2* pb = part + b * 64 + k;
   qrdf::df2 s = {0.f, 0.f};
-  int c = 0;
-  for (; c + 4 <= nchunk; c += 4) {
-    const qrdf::df2 p0 = part[int64_t(c) * 4096 + o], p1 = part[int64_t(c + 1) * 4096 + o],
-                    p2 = part[int64_t(c + 2) * 4096 + o], p3 = part[int64_t(c + 3) * 4096 + o];
+  int c = g;
+  for (; c + 12 < nchunk; c += 16) {
+    const qrdf::df2 p0 = pb[int64_t(c) * 4096], p1 = pb[int64_t(c + 4) * 4096], p2 = pb[int64_t(c + 8) * 4096],
+                    p3 = pb[int64_t(c + 12) * 4096];
     s = qrdf::add(s, p0);
     s = qrdf::add(s, p1);
     s = qrdf::add(s, p2);
     s = qrdf::add(s, p3);
   }
-  for (; c < nchunk; ++c) s = qrdf::add(s, part[int64_t(c) * 4096 + o]);
-  W[o] = s;
-}
-
-// W2[a][b] = sum_{k <= a} T(k, a) W[k][b]; one CTA of 64 threads per column b, T column-major
-// (ld NB), upper triangular
-__global__ void __launch_bounds__(64) nar_tmul_kernel(const qrdf::df2* __restrict__ W, int nb,
-                                                      const double* __restrict__ T, int NB,
-                                                      qrdf::df2* __restrict__ W2) {
-  __shared__ qrdf::df2 Ws[64];
-  const int b = blockIdx.x, a = threadIdx.x;
-  Ws[a] = W[a * 64 + b];
+  for (; c < nchunk; c += 4) s = qrdf::add(s, pb[int64_t(c) * 4096]);
+  Wg[g][k] = s;
   __syncthreads();
-  qrdf::df2 t = {0.f, 0.f};
-  if (a < nb)
-    for (int kk = 0; kk <= a; ++kk) {
-      qrdf::df2 tk;
-      split_df(T[a * NB + kk], tk.h, tk.l);
-      qrdf::acc(t, tk, Ws[kk]);
-    }
-  W2[a * 64 + b] = qrdf::norm(t);
+  if (tid < 64) {
+    Wg[0][k] = qrdf::add(qrdf::add(Wg[0][k], Wg[1][k]), qrdf::add(Wg[2][k], Wg[3][k]));
+  }
+  __syncthreads();
+  if (tid < 64) {
+    const int a = tid;
+    qrdf::df2 t = {0.f, 0.f};
+    if (a < nb)
+      for (int kk = 0; kk <= a; ++kk) {
+        qrdf::df2 tk;
+        split_df(Ts[a][kk], tk.h, tk.l);
+        qrdf::acc(t, tk, Wg[0][kk]);
+      }
+    W2[a * 64 + b] = qrdf::norm(t);
+  }
 }
 
 // C[r][b] -= sum_a V[r][a] W2[a][b] for the rows of one chunk
@@ -728,7 +738,12 @@ __global__ void __launch_bounds__(NR_T) nar_update_kernel(const double* __restri
   __shared__ qrdf::df2 Ws[64][65], Vs[NR_ROWS][65];
   const int tid = threadIdx.x;
   const int64_t r0 = int64_t(blockIdx.x) * NR_ROWS;
-  for (int e = tid; e < 64 * 64; e += NR_T) Ws[e / 64][e % 64] = W2[e];
+#pragma unroll
+  for (int i = 0; i < 64 * 64 / NR_T; ++i) {
+    const int e = tid + i * NR_T;
+    Ws[e / 64][e % 64] = W2[e];
+  }
+#pragma unroll
   for (int e = tid; e < NR_ROWS * 64; e += NR_T) {
     const int r = e % NR_ROWS, c = e / NR_ROWS;
     const int64_t gr = r0 + r;
@@ -759,16 +774,14 @@ __global__ void __launch_bounds__(NR_T) nar_update_kernel(const double* __restri
 }
 
 // C -= V T^T V^T C for a block of nc <= 64 columns (the next panel), double-FP32 arithmetic;
-// part holds ceil(mp / NR_ROWS) * 64 * 64 float pairs, W and W2 64 * 64 each
+// part holds ceil(mp / NR_ROWS) * 64 * 64 float pairs, W2 64 * 64
 int apply_panel_narrow(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int nc,
-                       qrdf::df2* W, qrdf::df2* W2, qrdf::df2* part, cudaStream_t st) {
+                       qrdf::df2* W2, qrdf::df2* part, cudaStream_t st) {
   const int nchunk = int((mp + NR_ROWS - 1) / NR_ROWS);
   profile_mark(KF_F64_GEMM, st, true);
   nar_partial_kernel<<<nchunk, NR_T, 0, st>>>(Vp, mp, nb, C, m, nc, part);
   TNX_LAUNCH_CHECK();
-  nar_reduce_kernel<<<16, 256, 0, st>>>(part, nchunk, W);
-  TNX_LAUNCH_CHECK();
-  nar_tmul_kernel<<<nc, 64, 0, st>>>(W, nb, Tp, NB, W2);
+  nar_reduce_kernel<<<nc, NRED_T, 0, st>>>(part, nchunk, nb, Tp, NB, W2);
   TNX_LAUNCH_CHECK();
   nar_update_kernel<<<nchunk, NR_T, 0, st>>>(Vp, mp, nb, W2, C, m, nc);
   TNX_LAUNCH_CHECK();
@@ -796,9 +809,13 @@ int apply_panel_t(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const
 
 // Look-ahead stream and its two events, one set per host thread and device, created on first use
 // and kept for the thread's lifetime.
+// `hi` (the highest stream priority) carries the factorisation's critical path (panels and the
+// next panel's update), `aux` (the lowest) the bulk trailing updates: when both have blocks
+// waiting, the SMs that free up go to the critical path first (a 16-CTA panel cluster needs 16
+// free SMs of one GPC at once).
 struct LookAhead {
-  cudaStream_t aux = nullptr;
-  cudaEvent_t ev_v = nullptr, ev_r = nullptr;
+  cudaStream_t aux = nullptr, hi = nullptr;
+  cudaEvent_t ev_v = nullptr, ev_r = nullptr, ev_h = nullptr;
 };
 
 int look_ahead(LookAhead** out) {
@@ -809,9 +826,13 @@ int look_ahead(LookAhead** out) {
   TNX_CHECK_ARG(dev >= 0 && dev < MAXDEV, "device index %d out of range", dev);
   LookAhead& l = la[dev];
   if (!l.aux) {
-    TNX_CUDA(cudaStreamCreateWithFlags(&l.aux, cudaStreamNonBlocking));
+    int least = 0, greatest = 0;
+    TNX_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    TNX_CUDA(cudaStreamCreateWithPriority(&l.aux, cudaStreamNonBlocking, least));
+    TNX_CUDA(cudaStreamCreateWithPriority(&l.hi, cudaStreamNonBlocking, greatest));
     TNX_CUDA(cudaEventCreateWithFlags(&l.ev_v, cudaEventDisableTiming));
     TNX_CUDA(cudaEventCreateWithFlags(&l.ev_r, cudaEventDisableTiming));
+    TNX_CUDA(cudaEventCreateWithFlags(&l.ev_h, cudaEventDisableTiming));
   }
   *out = &l;
   return TNX_OK;
@@ -821,11 +842,12 @@ int look_ahead(LookAhead** out) {
 
 // Factor the column-major m x n matrix in w.F (m >= n) and form Q (column-major) in w.Qc.
 //
-// Factorisation with look-ahead: after panel p is factored, the caller's stream updates only the
-// next panel's columns with H_p and factors panel p+1, while the look-ahead stream applies H_p to
-// all columns beyond panel p+1 (the bulk of the flops); the 16 SMs of a panel no longer leave
-// the rest of the GPU idle. Panel p+2's columns (part of that bulk) are used only after the
-// look-ahead stream's update of step p has completed. V is double-buffered between the streams.
+// Factorisation with look-ahead: after panel p is factored, a high-priority stream updates only
+// the next panel's columns with H_p and factors panel p+1, while the low-priority look-ahead
+// stream applies H_p to all columns beyond panel p+1 (the bulk of the flops); the 16 SMs of a
+// panel no longer leave the rest of the GPU idle. Panel p+2's columns (part of that bulk) are
+// used only after the look-ahead stream's update of step p has completed. V is double-buffered
+// between the streams; both join the caller's stream at the end.
 int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false, bool form_q = true) {
   const PanelPlan pp = plan_panels(m, df);
   const int NB = pp.nb;
@@ -833,10 +855,12 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
   const int64_t part_cap = int64_t(QR_SPLIT_MAX) * n * QBMAX;  // doubles of each split-K scratch
   LookAhead* la = nullptr;
   TNX_TRY(look_ahead(&la));
-  // the look-ahead stream starts after everything queued on the caller's stream
+  cudaStream_t cs = la->hi;  // critical path
+  // both streams start after everything queued on the caller's stream
   TNX_CUDA(cudaEventRecord(la->ev_r, st));
   TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_r, 0));
-  TNX_TRY(factor_panel(pp, w.F, m, 0, int(n < NB ? n : NB), w.tau, w.T, st));
+  TNX_CUDA(cudaStreamWaitEvent(cs, la->ev_r, 0));
+  TNX_TRY(factor_panel(pp, w.F, m, 0, int(n < NB ? n : NB), w.tau, w.T, cs));
   for (int64_t p = 0; p < np; ++p) {
     const int64_t j0 = p * NB;
     const int nb = int(n - j0 < NB ? n - j0 : NB);
@@ -844,34 +868,37 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
     const int64_t mp = m - j0, nc = n - j0 - nb;
     if (nc <= 0) break;
     double* Vp = (p & 1) ? w.Vp2 : w.Vp;
-    panel_v_kernel<<<blocks_for(mp * nb), 256, 0, st>>>(w.F, m, j0, nb, Vp);
+    panel_v_kernel<<<blocks_for(mp * nb), 256, 0, cs>>>(w.F, m, j0, nb, Vp);
     TNX_LAUNCH_CHECK();
     const int nb1 = int(nc < NB ? nc : NB);  // next panel
     const int64_t rest = nc - nb1;
     double* Cn = w.F + (j0 + nb) * m + j0;
     if (rest > 0) {
-      TNX_CUDA(cudaEventRecord(la->ev_v, st));  // V_p, T_p ready; panel p+2's columns updated by H_{p-1}
+      TNX_CUDA(cudaEventRecord(la->ev_v, cs));  // V_p, T_p ready; panel p+2's columns updated by H_{p-1}
       TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_v, 0));
       TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, part_cap,
                             la->aux, df));
     }
     const bool narrow = df && n >= 64 && (mp + NR_ROWS - 1) / NR_ROWS * 64 * 64 <= part_cap;
     if (narrow) {
-      TNX_TRY(apply_panel_narrow(m, mp, nb, NB, Vp, Tp, Cn, nb1, reinterpret_cast<qrdf::df2*>(w.W1),
-                                 reinterpret_cast<qrdf::df2*>(w.W2), reinterpret_cast<qrdf::df2*>(w.part), st));
+      TNX_TRY(apply_panel_narrow(m, mp, nb, NB, Vp, Tp, Cn, nb1, reinterpret_cast<qrdf::df2*>(w.W2),
+                                 reinterpret_cast<qrdf::df2*>(w.part), cs));
     } else {
-      TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, st, df));
+      TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, cs, df));
     }
-    TNX_TRY(factor_panel(pp, w.F, m, j0 + nb, nb1, w.tau + (p + 1) * NB, w.T + (p + 1) * NB * NB, st));
+    TNX_TRY(factor_panel(pp, w.F, m, j0 + nb, nb1, w.tau + (p + 1) * NB, w.T + (p + 1) * NB * NB, cs));
     if (rest > 0) {
       // the next step reads panel p+2's columns and rewrites the other V buffer
       TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));
-      TNX_CUDA(cudaStreamWaitEvent(st, la->ev_r, 0));
+      TNX_CUDA(cudaStreamWaitEvent(cs, la->ev_r, 0));
     }
   }
-  // join the look-ahead stream back (also when it received no work: keeps stream capture balanced)
+  // join both streams back into the caller's (also when they received no work: keeps stream
+  // capture balanced)
   TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));
   TNX_CUDA(cudaStreamWaitEvent(st, la->ev_r, 0));
+  TNX_CUDA(cudaEventRecord(la->ev_h, cs));
+  TNX_CUDA(cudaStreamWaitEvent(st, la->ev_h, 0));
   if (!form_q) return TNX_OK;
   // Q = H_0 H_1 ... [I; 0]: apply panels last to first to the columns >= j0
   eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.Qc, m, n);
