@@ -430,17 +430,6 @@ unsigned blocks_for(int64_t total) {
   return unsigned(b < 1 ? 1 : b);
 }
 
-// Tf (row-major n x n): the panel T factors (column-major NB x NB each, in T) on the diagonal
-// blocks, zero elsewhere
-__global__ void t_diag_kernel(const double* __restrict__ T, int64_t n, int NB, double* __restrict__ Tf) {
-  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < n * n; e += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t r = e / n, c = e % n, p = r / NB;
-    double v = 0.0;
-    if (r <= c && c / NB == p) v = T[p * NB * NB + (c - p * NB) * NB + (r - p * NB)];
-    Tf[e] = v;
-  }
-}
-
 // Two scratch sets (Vp / W1 / W2 / part): set 0 for the caller's stream, set 1 for the
 // look-ahead stream of the factorisation.
 struct QrWs {
@@ -647,7 +636,7 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
 // all rows of the GPU instead: NR_ROWS-row chunks of V^T C per CTA, a fixed-order reduction of
 // the chunk partials fused with T^T W, and the rank-nb update per row chunk.
 constexpr int NR_ROWS = 16;   // rows of V and C per CTA in the partial and update kernels
-constexpr int NR_T = 256;     // threads of those kernels
+constexpr int NR_T = 512;     // threads of those kernels
 
 // part[c][b][a] = sum over rows r of chunk c of V[r][a] C[r][b]  (a < nb, b < nc <= 64; df2)
 __global__ void __launch_bounds__(NR_T) nar_partial_kernel(const double* __restrict__ Vp, int64_t mp, int nb,
@@ -669,19 +658,20 @@ __global__ void __launch_bounds__(NR_T) nar_partial_kernel(const double* __restr
     Cs[r][c] = x;
   }
   __syncthreads();
-  const int a = tid & 63, bq = tid >> 6;  // outputs (a, bq + 4 j)
-  qrdf::df2 acc[16];
+  constexpr int PJ = 64 * 64 / NR_T, PS = NR_T / 64;  // outputs per thread, their column stride
+  const int a = tid & 63, bq = tid >> 6;              // outputs (a, bq + PS j)
+  qrdf::df2 acc[PJ];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) acc[j] = {0.f, 0.f};
+  for (int j = 0; j < PJ; ++j) acc[j] = {0.f, 0.f};
 #pragma unroll 4
   for (int r = 0; r < NR_ROWS; ++r) {
     const qrdf::df2 v = Vs[r][a];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) qrdf::acc(acc[j], v, Cs[r][bq + 4 * j]);
+    for (int j = 0; j < PJ; ++j) qrdf::acc(acc[j], v, Cs[r][bq + PS * j]);
   }
   qrdf::df2* out = part + int64_t(blockIdx.x) * 64 * 64;
 #pragma unroll
-  for (int j = 0; j < 16; ++j) out[(bq + 4 * j) * 64 + a] = qrdf::norm(acc[j]);
+  for (int j = 0; j < PJ; ++j) out[(bq + PS * j) * 64 + a] = qrdf::norm(acc[j]);
 }
 
 // W2[a][b] = sum_{k <= a} T(k, a) W[k][b] with W[k][b] = sum over chunks c of part[c][b][k]; one
@@ -752,20 +742,21 @@ __global__ void __launch_bounds__(NR_T) nar_update_kernel(const double* __restri
     Vs[r][c] = v;
   }
   __syncthreads();
-  const int r = tid % NR_ROWS, bq = tid / NR_ROWS;  // outputs (r, bq + 16 j)
-  qrdf::df2 acc[4];
+  constexpr int UJ = NR_ROWS * 64 / NR_T, US = NR_T / NR_ROWS;  // outputs per thread, column stride
+  const int r = tid % NR_ROWS, bq = tid / NR_ROWS;              // outputs (r, bq + US j)
+  qrdf::df2 acc[UJ];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) acc[j] = {0.f, 0.f};
+  for (int j = 0; j < UJ; ++j) acc[j] = {0.f, 0.f};
   for (int a = 0; a < nb; ++a) {
     const qrdf::df2 v = Vs[r][a];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) qrdf::acc(acc[j], v, Ws[a][bq + 16 * j]);
+    for (int j = 0; j < UJ; ++j) qrdf::acc(acc[j], v, Ws[a][bq + US * j]);
   }
   const int64_t gr = r0 + r;
   if (gr < mp)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int b = bq + 16 * j;
+    for (int j = 0; j < UJ; ++j) {
+      const int b = bq + US * j;
       if (b < nc) {
         const qrdf::df2 s = qrdf::norm(acc[j]);
         C[int64_t(b) * ldc + gr] -= join_df(s.h, s.l);
@@ -810,12 +801,13 @@ int apply_panel_t(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const
 // Look-ahead stream and its two events, one set per host thread and device, created on first use
 // and kept for the thread's lifetime.
 // `hi` (the highest stream priority) carries the factorisation's critical path (panels and the
-// next panel's update), `aux` (the lowest) the bulk trailing updates: when both have blocks
-// waiting, the SMs that free up go to the critical path first (a 16-CTA panel cluster needs 16
-// free SMs of one GPC at once).
+// next panel's update), `aux` (a middle priority) the bulk trailing updates, `wy` (the lowest)
+// the compact-WY bookkeeping of the FP64-class gauge move: when several have blocks waiting,
+// the SMs that free up go to the critical path first (a 16-CTA panel cluster needs 16 free SMs
+// of one GPC at once).
 struct LookAhead {
-  cudaStream_t aux = nullptr, hi = nullptr;
-  cudaEvent_t ev_v = nullptr, ev_r = nullptr, ev_h = nullptr;
+  cudaStream_t aux = nullptr, hi = nullptr, wy = nullptr;
+  cudaEvent_t ev_v = nullptr, ev_r = nullptr, ev_h = nullptr, ev_w = nullptr;
 };
 
 int look_ahead(LookAhead** out) {
@@ -828,17 +820,106 @@ int look_ahead(LookAhead** out) {
   if (!l.aux) {
     int least = 0, greatest = 0;
     TNX_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    TNX_CUDA(cudaStreamCreateWithPriority(&l.aux, cudaStreamNonBlocking, least));
     TNX_CUDA(cudaStreamCreateWithPriority(&l.hi, cudaStreamNonBlocking, greatest));
+    TNX_CUDA(cudaStreamCreateWithPriority(&l.aux, cudaStreamNonBlocking, (least + greatest) / 2));
+    TNX_CUDA(cudaStreamCreateWithPriority(&l.wy, cudaStreamNonBlocking, least));
     TNX_CUDA(cudaEventCreateWithFlags(&l.ev_v, cudaEventDisableTiming));
     TNX_CUDA(cudaEventCreateWithFlags(&l.ev_r, cudaEventDisableTiming));
     TNX_CUDA(cudaEventCreateWithFlags(&l.ev_h, cudaEventDisableTiming));
+    TNX_CUDA(cudaEventCreateWithFlags(&l.ev_w, cudaEventDisableTiming));
   }
   *out = &l;
   return TNX_OK;
 }
 
 }  // namespace
+
+// ---- Q from the compact WY form of all n reflectors (FP64-class modes, large QRs) ----------
+//
+// H_0 H_1 ... H_{n-1} = I - V Tf V^T with V (m x n, unit lower trapezoidal) and Tf (n x n, upper
+// triangular). Tf grows by one panel per factorisation step, on the look-ahead stream while the
+// next panels are factored (dlarft's recurrence applied a panel at a time):
+//   Tf[0:j0, p] = -Tf[0:j0, 0:j0] (V[:, 0:j0]^T V_p) T_p,   Tf[p, p] = T_p,
+// so that only the last panel's column block is left when the factorisation ends. Then
+//   Q = [I; 0] - V (Tf V_top^T),   V_top = rows 0..n-1 of V,
+// two FP64-class GEMMs on the tensor cores (Ozaki). The backward accumulation this replaces is
+// 16 steps of narrow K = 64 products on the FP32 pipe after the factorisation.
+struct WyWs {
+  double *V, *S, *Tf, *X, *Y;  // S: the n x 64 block V^T V_p of the current step, Y: S T_p
+  double* part;                // split-K scratch of the V^T V_p products
+  void* oz;
+  size_t oz_bytes;
+};
+
+inline bool wy_applies(int64_t m, int64_t n, bool df) { return df && use_oz(n, n, m) && n >= 256; }
+
+size_t wy_oz_bytes(int64_t m, int64_t n) {
+  size_t b = gemm_oz_workspace_bytes(n, n, n);  // X
+  auto mx = [&](size_t x) { b = x > b ? x : b; };
+  mx(gemm_oz_workspace_bytes(m, n, n));  // Q, row-major output
+  mx(gemm_oz_workspace_bytes(n, m, n));  // Q, column-major output
+  return b;
+}
+
+size_t wy_layout(int64_t m, int64_t n, void* base, WyWs* w) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += align_up(bytes); return o; };
+  const size_t oV = take(size_t(m) * n * 8), oS = take(size_t(n) * n * 8), oT = take(size_t(n) * n * 8),
+               oX = take(size_t(n) * n * 8), oY = take(size_t(n) * n * 8 / 4),
+               oP = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8), obz = wy_oz_bytes(m, n), oZ = take(obz);
+  if (w && base) {
+    char* b = static_cast<char*>(base);
+    w->V = reinterpret_cast<double*>(b + oV);
+    w->S = reinterpret_cast<double*>(b + oS);
+    w->Tf = reinterpret_cast<double*>(b + oT);
+    w->X = reinterpret_cast<double*>(b + oX);
+    w->Y = reinterpret_cast<double*>(b + oY);
+    w->part = reinterpret_cast<double*>(b + oP);
+    w->oz = b + oZ;
+    w->oz_bytes = obz;
+  }
+  return off;
+}
+
+// V column block p (full height, ld m: zero above the diagonal, unit diagonal) from F
+__global__ void v_block_kernel(const double* __restrict__ F, int64_t m, int64_t j0, int nb, double* __restrict__ V) {
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < m * nb; e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = j0 + e / m, r = e % m;
+    V[c * m + r] = r < c ? 0.0 : (r == c ? 1.0 : F[c * m + r]);
+  }
+}
+
+// Tf diagonal block p (row-major, ld n) = T_p (column-major, ld NB), zero below its diagonal
+__global__ void t_block_kernel(const double* __restrict__ Tp, int NB, int nb, double* __restrict__ Tf, int64_t n,
+                               int64_t j0) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb * nb; e += gridDim.x * blockDim.x) {
+    const int a = e / nb, b = e % nb;
+    Tf[(j0 + a) * n + j0 + b] = a <= b ? Tp[b * NB + a] : 0.0;
+  }
+}
+
+// Append panel p (columns j0 .. j0+nb) to V and Tf: V's column block, then
+// Tf[0:j0, j0:j0+nb] = -Tf[0:j0, 0:j0] (V[:, 0:j0]^T V_p) T_p and the diagonal block T_p.
+// part: split-K scratch of at least QR_SPLIT_MAX * n * QBMAX doubles.
+int wy_append_panel(int64_t m, int64_t n, int NB, int64_t j0, int nb, const double* F, const double* Tp,
+                    const WyWs& y, double* part, cudaStream_t st) {
+  v_block_kernel<<<blocks_for(m * nb), 256, 0, st>>>(F, m, j0, nb, y.V);
+  TNX_LAUNCH_CHECK();
+  t_block_kernel<<<(nb * nb + 255) / 256, 256, 0, st>>>(Tp, NB, nb, y.Tf, n, j0);
+  TNX_LAUNCH_CHECK();
+  if (j0 == 0) return TNX_OK;
+  // S (j0 x nb, ld nb) = V[:, 0:j0]^T V_p over rows >= j0, where V_p is nonzero
+  // (op(A)(i, k) = V(j0 + k, i); op(B)(k, j) = V(j0 + k, j0 + j))
+  const int64_t K = m - j0;
+  TNX_TRY(gemm_f64_splitk(false, true, j0, nb, K, 1.0, y.V + j0, m, y.V + j0 * m + j0, m, 0.0, y.S, nb,
+                          qr_nsplit_cap(K, j0, nb, int64_t(QR_SPLIT_MAX) * n * QBMAX), part, st, true));
+  // Y (j0 x nb, ld nb) = S T_p   (op(B)(k, j) = T_p(k, j) = Tp[j NB + k])
+  TNX_TRY(gemm_fp64_class(true, false, true, j0, nb, nb, 1.0, y.S, nb, 0, Tp, NB, 0, 0.0, y.Y, nb, 0, 1, st));
+  // Tf[0:j0, j0:j0+nb] = -Tf[0:j0, 0:j0] Y  (K = j0 long, nb = 64 wide: split over K)
+  TNX_TRY(gemm_f64_splitk(false, false, j0, nb, j0, -1.0, y.Tf, n, y.Y, nb, 0.0, y.Tf + j0, n,
+                          qr_nsplit_cap(j0, j0, nb, int64_t(QR_SPLIT_MAX) * n * QBMAX), y.part, st, true));
+  return TNX_OK;
+}
 
 // Factor the column-major m x n matrix in w.F (m >= n) and form Q (column-major) in w.Qc.
 //
@@ -848,7 +929,8 @@ int look_ahead(LookAhead** out) {
 // panel no longer leave the rest of the GPU idle. Panel p+2's columns (part of that bulk) are
 // used only after the look-ahead stream's update of step p has completed. V is double-buffered
 // between the streams; both join the caller's stream at the end.
-int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false, bool form_q = true) {
+int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false, bool form_q = true,
+                const WyWs* wy = nullptr) {
   const PanelPlan pp = plan_panels(m, df);
   const int NB = pp.nb;
   const int64_t np = (n + NB - 1) / NB;
@@ -860,6 +942,10 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
   TNX_CUDA(cudaEventRecord(la->ev_r, st));
   TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_r, 0));
   TNX_CUDA(cudaStreamWaitEvent(cs, la->ev_r, 0));
+  if (wy) {
+    TNX_CUDA(cudaStreamWaitEvent(la->wy, la->ev_r, 0));
+    TNX_CUDA(cudaMemsetAsync(wy->Tf, 0, size_t(n) * n * 8, la->wy));
+  }
   TNX_TRY(factor_panel(pp, w.F, m, 0, int(n < NB ? n : NB), w.tau, w.T, cs));
   for (int64_t p = 0; p < np; ++p) {
     const int64_t j0 = p * NB;
@@ -873,11 +959,17 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
     const int nb1 = int(nc < NB ? nc : NB);  // next panel
     const int64_t rest = nc - nb1;
     double* Cn = w.F + (j0 + nb) * m + j0;
+    if (rest > 0 || wy) TNX_CUDA(cudaEventRecord(la->ev_v, cs));  // V_p, T_p ready; panel p+2's columns updated
     if (rest > 0) {
-      TNX_CUDA(cudaEventRecord(la->ev_v, cs));  // V_p, T_p ready; panel p+2's columns updated by H_{p-1}
       TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_v, 0));
       TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, part_cap,
                             la->aux, df));
+      TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));  // panel p+2's columns updated by H_p
+    }
+    // panel p joins the compact WY form on the lowest-priority stream, off the critical path
+    if (wy) {
+      TNX_CUDA(cudaStreamWaitEvent(la->wy, la->ev_v, 0));
+      TNX_TRY(wy_append_panel(m, n, NB, j0, nb, w.F, Tp, *wy, wy->part, la->wy));
     }
     const bool narrow = df && n >= 64 && (mp + NR_ROWS - 1) / NR_ROWS * 64 * 64 <= part_cap;
     if (narrow) {
@@ -887,11 +979,8 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
       TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn, nb1, w.W1, w.W2, w.part, part_cap, cs, df));
     }
     TNX_TRY(factor_panel(pp, w.F, m, j0 + nb, nb1, w.tau + (p + 1) * NB, w.T + (p + 1) * NB * NB, cs));
-    if (rest > 0) {
-      // the next step reads panel p+2's columns and rewrites the other V buffer
-      TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));
-      TNX_CUDA(cudaStreamWaitEvent(cs, la->ev_r, 0));
-    }
+    // the next step reads panel p+2's columns and rewrites the other V buffer
+    if (rest > 0) TNX_CUDA(cudaStreamWaitEvent(cs, la->ev_r, 0));
   }
   // join both streams back into the caller's (also when they received no work: keeps stream
   // capture balanced)
@@ -899,6 +988,12 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
   TNX_CUDA(cudaStreamWaitEvent(st, la->ev_r, 0));
   TNX_CUDA(cudaEventRecord(la->ev_h, cs));
   TNX_CUDA(cudaStreamWaitEvent(st, la->ev_h, 0));
+  if (wy) {  // the WY stream's work so far, then the last panel
+    TNX_CUDA(cudaEventRecord(la->ev_w, la->wy));
+    TNX_CUDA(cudaStreamWaitEvent(st, la->ev_w, 0));
+    const int64_t j0 = (np - 1) * NB;
+    TNX_TRY(wy_append_panel(m, n, NB, j0, int(n - j0), w.F, w.T + (np - 1) * NB * NB, *wy, wy->part, st));
+  }
   if (!form_q) return TNX_OK;
   // Q = H_0 H_1 ... [I; 0]: apply panels last to first to the columns >= j0
   eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.Qc, m, n);
@@ -922,104 +1017,32 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
   return TNX_OK;
 }
 
-// ---- Q from the compact WY form of all n reflectors (FP64-class modes, large QRs) ----------
-//
-// H_0 H_1 ... H_{n-1} = I - V Tf V^T with V (m x n, unit lower trapezoidal) and Tf (n x n, upper
-// triangular). Tf is assembled from the panel T factors by the block recurrence
-//   Tf = [[T_A, -T_A (V_A^T V_B) T_B], [0, T_B]]
-// applied to pairs of neighbouring blocks of doubling width (64, 128, 256, 512), with the Gram
-// matrix S = V^T V from one FP64-class tensor-core GEMM. Then
-//   Q = [I; 0] - V (Tf V_top^T),   V_top = rows 0..n-1 of V,
-// two more GEMMs. Every product with more than 2^27 multiply-adds runs on the Ozaki GEMM; the
-// backward accumulation it replaces is 16 steps of narrow K = 64 products on the FP32 pipe.
-struct WyWs {
-  double *V, *S, *Tf, *X, *Y;
-  void* oz;
-  size_t oz_bytes;
-};
-
-inline bool wy_applies(int64_t m, int64_t n, bool df) { return df && use_oz(n, n, m) && n >= 256; }
-
-size_t wy_oz_bytes(int64_t m, int64_t n) {
-  size_t b = gemm_oz_workspace_bytes(n, n, m);  // S
-  auto mx = [&](size_t x) { b = x > b ? x : b; };
-  mx(gemm_oz_workspace_bytes(n, n, n));  // X
-  mx(gemm_oz_workspace_bytes(m, n, n));  // Q, row-major output
-  mx(gemm_oz_workspace_bytes(n, m, n));  // Q, column-major output
-  return b;
+// FP64-class product on the Ozaki GEMM without the autotuner (the gauge move runs the Q
+// formation and the R A product concurrently, which would distort a first-call timing); the
+// autotuned path where the Ozaki GEMM does not apply
+int gemm_oz_direct(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+                   const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* oz, size_t ozb,
+                   cudaStream_t st) {
+  if (oz && use_oz(m, n, k) && ozb >= gemm_oz_workspace_bytes(m, n, k))
+    return gemm_oz(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, oz, ozb, st);
+  return gemm_fp64_class_oz(true, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, oz, ozb, st);
 }
 
-size_t wy_layout(int64_t m, int64_t n, void* base, WyWs* w) {
-  size_t off = 0;
-  auto take = [&](size_t bytes) { size_t o = off; off += align_up(bytes); return o; };
-  const size_t oV = take(size_t(m) * n * 8), oS = take(size_t(n) * n * 8), oT = take(size_t(n) * n * 8),
-               oX = take(size_t(n) * n * 8), oY = take(size_t(n) * n * 8 / 4), obz = wy_oz_bytes(m, n),
-               oZ = take(obz);
-  if (w && base) {
-    char* b = static_cast<char*>(base);
-    w->V = reinterpret_cast<double*>(b + oV);
-    w->S = reinterpret_cast<double*>(b + oS);
-    w->Tf = reinterpret_cast<double*>(b + oT);
-    w->X = reinterpret_cast<double*>(b + oX);
-    w->Y = reinterpret_cast<double*>(b + oY);
-    w->oz = b + oZ;
-    w->oz_bytes = obz;
-  }
-  return off;
-}
-
-// Q (m x n) from the factorisation in w.F / w.T: row-major (ld n) when q_rowmajor, otherwise
-// column-major (ld m)
-int form_q_wy(int64_t m, int64_t n, int NB, const QrWs& w, const WyWs& y, double* Q, bool q_rowmajor,
-              cudaStream_t st) {
-  // V column-major (ld m): row-major view V^T (n x m, ld m)
-  panel_v_kernel<<<blocks_for(m * n), 256, 0, st>>>(w.F, m, 0, int(n), y.V);
-  TNX_LAUNCH_CHECK();
-  t_diag_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.T, n, NB, y.Tf);
-  TNX_LAUNCH_CHECK();
-  // S = V^T V (row-major n x n)
-  TNX_TRY(gemm_fp64_class_oz(true, false, true, n, n, m, 1.0, y.V, m, y.V, m, 0.0, y.S, n, y.oz, y.oz_bytes, st));
-  // Tf_AB = -Tf_A S_AB Tf_B for neighbouring blocks A = [a0, a0 + b), B = [a0 + b, a0 + 2b)
-  for (int64_t b = NB; b < n; b *= 2) {
-    const int64_t full = n / (2 * b);  // pairs with both blocks complete
-    const int64_t stride = 2 * b * (n + 1);
-    if (full > 0) {
-      if (use_oz(b, b, b)) {
-        for (int64_t i = 0; i < full; ++i) {
-          const int64_t a0 = 2 * b * i, b0 = a0 + b;
-          TNX_TRY(gemm_fp64_class_oz(true, false, false, b, b, b, 1.0, y.S + a0 * n + b0, n, y.Tf + b0 * n + b0, n,
-                                     0.0, y.Y, b, y.oz, y.oz_bytes, st));
-          TNX_TRY(gemm_fp64_class_oz(true, false, false, b, b, b, -1.0, y.Tf + a0 * n + a0, n, y.Y, b, 0.0,
-                                     y.Tf + a0 * n + b0, n, y.oz, y.oz_bytes, st));
-        }
-      } else {
-        TNX_TRY(gemm_fp64_class(true, false, false, b, b, b, 1.0, y.S + b, n, stride, y.Tf + b * n + b, n, stride, 0.0,
-                                y.Y, b, b * b, full, st));
-        TNX_TRY(gemm_fp64_class(true, false, false, b, b, b, -1.0, y.Tf, n, stride, y.Y, b, b * b, 0.0, y.Tf + b, n,
-                                stride, full, st));
-      }
-    }
-    const int64_t a0 = 2 * b * full, b0 = a0 + b;
-    if (b0 < n) {  // trailing pair with a short B block
-      const int64_t nbB = n - b0;
-      TNX_TRY(gemm_fp64_class(true, false, false, b, nbB, nbB, 1.0, y.S + a0 * n + b0, n, 0, y.Tf + b0 * n + b0, n,
-                              0, 0.0, y.Y, nbB, 0, 1, st));
-      TNX_TRY(gemm_fp64_class(true, false, false, b, nbB, b, -1.0, y.Tf + a0 * n + a0, n, 0, y.Y, nbB, 0, 0.0,
-                              y.Tf + a0 * n + b0, n, 0, 1, st));
-    }
-  }
+// Q (m x n) from V and Tf (built during the factorisation): row-major (ld n) when q_rowmajor,
+// otherwise column-major (ld m)
+int form_q_wy(int64_t m, int64_t n, const WyWs& y, double* Q, bool q_rowmajor, cudaStream_t st) {
   // X = Tf V_top^T  (op(B)(k, j) = V(j, k) = V[k m + j])
-  TNX_TRY(gemm_fp64_class_oz(true, false, false, n, n, n, 1.0, y.Tf, n, y.V, m, 0.0, y.X, n, y.oz, y.oz_bytes, st));
+  TNX_TRY(gemm_oz_direct(false, false, n, n, n, 1.0, y.Tf, n, y.V, m, 0.0, y.X, n, y.oz, y.oz_bytes, st));
   if (q_rowmajor) {
     // Q = [I; 0] - V X  (op(A)(i, k) = V(i, k) = V[k m + i])
     eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(Q, n, m);
     TNX_LAUNCH_CHECK();
-    TNX_TRY(gemm_fp64_class_oz(true, true, false, m, n, n, -1.0, y.V, m, y.X, n, 1.0, Q, n, y.oz, y.oz_bytes, st));
+    TNX_TRY(gemm_oz_direct(true, false, m, n, n, -1.0, y.V, m, y.X, n, 1.0, Q, n, y.oz, y.oz_bytes, st));
   } else {
     // Q^T = [I, 0] - X^T V^T  (row-major n x m)
     eye_kernel<<<blocks_for(m * n), 256, 0, st>>>(Q, m, n);
     TNX_LAUNCH_CHECK();
-    TNX_TRY(gemm_fp64_class_oz(true, true, false, n, m, n, -1.0, y.X, n, y.V, m, 1.0, Q, m, y.oz, y.oz_bytes, st));
+    TNX_TRY(gemm_oz_direct(true, false, n, m, n, -1.0, y.X, n, y.V, m, 1.0, Q, m, y.oz, y.oz_bytes, st));
   }
   return TNX_OK;
 }
@@ -1101,42 +1124,65 @@ int tnx_gauge_move(int direction, double* A_site, double* A_nb, int64_t chi_l, i
   const bool wy = wy_applies(m, n, df);
   WyWs wys{};
   if (wy) wy_layout(m, n, after_tmp + align_up(gauge_oz_bytes(direction, chi_l, d, chi_r, chi_other)), &wys);
-  const int NB = plan_panels(m, df).nb;
   cudaStream_t st = as_stream(stream);
   dim3 tb(32, 8);
   if (direction == 1) {
     // psi (chi_l d x chi_r) row-major -> column-major
     transpose_kernel<<<dim3(unsigned((n + 31) / 32), unsigned((m + 31) / 32)), tb, 0, st>>>(A_site, m, n, w.F);
     TNX_LAUNCH_CHECK();
-    TNX_TRY(qr_colmajor(m, n, w, st, df, !wy));
+    TNX_TRY(qr_colmajor(m, n, w, st, df, !wy, wy ? &wys : nullptr));
+    const int64_t nc = d * chi_other;
     if (wy) {
-      TNX_TRY(form_q_wy(m, n, NB, w, wys, A_site, true, st));
+      // A_next (chi_r x d chi_other) <- R A_next on the look-ahead stream while Q forms on the
+      // caller's stream
+      LookAhead* la = nullptr;
+      TNX_TRY(look_ahead(&la));
+      TNX_CUDA(cudaEventRecord(la->ev_r, st));
+      TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_r, 0));
+      extract_r_kernel<<<blocks_for(n * n), 256, 0, la->aux>>>(w.F, m, n, Rb);
+      TNX_LAUNCH_CHECK();
+      TNX_TRY(gemm_oz_direct(false, false, n, nc, n, 1.0, Rb, n, A_nb, nc, 0.0, tmp, nc, oz, ozb, la->aux));
+      TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, n * nc * 8, cudaMemcpyDeviceToDevice, la->aux));
+      TNX_TRY(form_q_wy(m, n, wys, A_site, true, st));
+      TNX_CUDA(cudaEventRecord(la->ev_v, la->aux));
+      TNX_CUDA(cudaStreamWaitEvent(st, la->ev_v, 0));
     } else {
       transpose_kernel<<<dim3(unsigned((m + 31) / 32), unsigned((n + 31) / 32)), tb, 0, st>>>(w.Qc, n, m, A_site);
       TNX_LAUNCH_CHECK();
+      extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
+      TNX_LAUNCH_CHECK();
+      // A_next (chi_r x d chi_other) <- R A_next
+      TNX_TRY(gemm_fp64_class_oz(df, false, false, n, nc, n, 1.0, Rb, n, A_nb, nc, 0.0, tmp, nc, oz, ozb, st));
+      TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, n * nc * 8, cudaMemcpyDeviceToDevice, st));
     }
-    extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
-    TNX_LAUNCH_CHECK();
-    // A_next (chi_r x d chi_other) <- R A_next
-    const int64_t nc = d * chi_other;
-    TNX_TRY(gemm_fp64_class_oz(df, false, false, n, nc, n, 1.0, Rb, n, A_nb, nc, 0.0, tmp, nc, oz, ozb, st));
-    TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, n * nc * 8, cudaMemcpyDeviceToDevice, st));
   } else {
     // psi (chi_l x d chi_r) row-major == psi^T (d chi_r x chi_l) column-major
     TNX_CUDA(cudaMemcpyAsync(w.F, A_site, m * n * 8, cudaMemcpyDeviceToDevice, st));
-    TNX_TRY(qr_colmajor(m, n, w, st, df, !wy));
+    TNX_TRY(qr_colmajor(m, n, w, st, df, !wy, wy ? &wys : nullptr));
+    const int64_t mr = chi_other * d;
     // Q column-major (d chi_r x chi_l) == Q^T row-major (chi_l x d chi_r)
     if (wy) {
-      TNX_TRY(form_q_wy(m, n, NB, w, wys, A_site, false, st));
+      // A_prev (chi_other d x chi_l) <- A_prev R^T on the look-ahead stream while Q forms on the
+      // caller's stream
+      LookAhead* la = nullptr;
+      TNX_TRY(look_ahead(&la));
+      TNX_CUDA(cudaEventRecord(la->ev_r, st));
+      TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_r, 0));
+      extract_r_kernel<<<blocks_for(n * n), 256, 0, la->aux>>>(w.F, m, n, Rb);
+      TNX_LAUNCH_CHECK();
+      TNX_TRY(gemm_oz_direct(false, true, mr, n, n, 1.0, A_nb, n, Rb, n, 0.0, tmp, n, oz, ozb, la->aux));
+      TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, mr * n * 8, cudaMemcpyDeviceToDevice, la->aux));
+      TNX_TRY(form_q_wy(m, n, wys, A_site, false, st));
+      TNX_CUDA(cudaEventRecord(la->ev_v, la->aux));
+      TNX_CUDA(cudaStreamWaitEvent(st, la->ev_v, 0));
     } else {
       TNX_CUDA(cudaMemcpyAsync(A_site, w.Qc, m * n * 8, cudaMemcpyDeviceToDevice, st));
+      extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
+      TNX_LAUNCH_CHECK();
+      // A_prev (chi_other d x chi_l) <- A_prev R^T
+      TNX_TRY(gemm_fp64_class_oz(df, false, true, mr, n, n, 1.0, A_nb, n, Rb, n, 0.0, tmp, n, oz, ozb, st));
+      TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, mr * n * 8, cudaMemcpyDeviceToDevice, st));
     }
-    extract_r_kernel<<<blocks_for(n * n), 256, 0, st>>>(w.F, m, n, Rb);
-    TNX_LAUNCH_CHECK();
-    // A_prev (chi_other d x chi_l) <- A_prev R^T
-    const int64_t mr = chi_other * d;
-    TNX_TRY(gemm_fp64_class_oz(df, false, true, mr, n, n, 1.0, A_nb, n, Rb, n, 0.0, tmp, n, oz, ozb, st));
-    TNX_CUDA(cudaMemcpyAsync(A_nb, tmp, mr * n * 8, cudaMemcpyDeviceToDevice, st));
   }
   return TNX_OK;
 }
