@@ -6,6 +6,10 @@
     python -m tnpy_gb300.prof gauge --chi 1024       # one-site gauge move (QR with double-FP32 GEMMs)
     python -m tnpy_gb300.prof davidson --chi 512     # one mixed-precision local eigensolve
     python -m tnpy_gb300.prof sweep --chi 1024 --sites 100   # fDMRG sweeps of XXZ(n, -0.5), per family
+    python -m tnpy_gb300.prof tsdrg --sites 128 --chi 32 --batch 64   # batched tSDRG realisations
+    python -m tnpy_gb300.prof chains --sites 64 --chi 64 --batch 64   # lockstep fDMRG chains, one sweep
+    python -m tnpy_gb300.prof svd --m 2048 --n 1024   # one-sided Jacobi SVD
+    python -m tnpy_gb300.prof ed --sites 12           # dense MPO Hamiltonian + full spectrum
 
 Each mode runs two warm-up calls and then --reps calls of the same shapes, on random seeded
 inputs, and prints the CUDA-event time per call and its split over the library's kernel
@@ -59,7 +63,9 @@ def _fmt(fam):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("mode", choices=["matvec", "env", "qr", "gauge", "davidson", "sweep"])
+    p.add_argument("mode", choices=["matvec", "env", "qr", "gauge", "davidson", "sweep", "tsdrg", "chains", "svd",
+                                    "ed"])
+    p.add_argument("--batch", type=int, default=64)
     p.add_argument("--sites", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--chi", type=int, default=1024)
@@ -88,6 +94,46 @@ def main(argv=None):
         t = _time(sweep, a.reps)
         fam = _families(sweep, 1)
         print(f"sweep XXZ({a.sites}) chi={chi}: {t:.1f} ms per sweep; one sweep per family: " + _fmt(fam))
+        return
+    if a.mode == "tsdrg":
+        import tnpy_gb300 as tg
+
+        mpos = [tg.model.RandomCouplingHeisenberg(a.sites, delta=1.0, h=0.0, seed=r).mpo for r in range(a.batch)]
+
+        def run():
+            tg.BatchedTSDRG(mpos, chi=chi).run()
+
+        t = _time(run, a.reps)
+        print(f"tsdrg n={a.sites} chi={chi} x{a.batch}: {t:.1f} ms per batch ({a.batch / t * 1e3:.1f} realisations/s)")
+        return
+    if a.mode == "chains":
+        import tnpy_gb300 as tg
+
+        mpos = [tg.model.RandomHeisenberg(a.sites, h=1.0, seed=100 + c).mpo for c in range(a.batch)]
+        b = tg.BatchedFiniteDMRG(mpos, bond_dim=chi, seed=100, precision="mixed", device=dev)
+        dirs = [tg.Direction.RIGHTWARD, tg.Direction.LEFTWARD]
+        step = [0]
+
+        def sweep():
+            b.sweep(dirs[step[0] % 2], tol=1e-8)
+            step[0] += 1
+
+        for _ in range(a.warmup):
+            sweep()
+        t = _time(sweep, a.reps)
+        print(f"chains n={a.sites} chi={chi} x{a.batch}: {t:.1f} ms per lockstep sweep")
+        return
+    if a.mode == "svd":
+        m = rnd(a.m, a.n)
+        t = _time(lambda: K.svd(m), a.reps)
+        print(f"svd {a.m}x{a.n}: {t:.3f} ms")
+        return
+    if a.mode == "ed":
+        import tnpy_gb300 as tg
+
+        mpo = tg.model.RandomHeisenberg(a.sites, h=0.5, seed=1).mpo
+        t = _time(lambda: tg.ExactDiagonalization(mpo, device=dev), a.reps)
+        print(f"exact diagonalisation n={a.sites}: {t:.1f} ms")
         return
     if a.mode in ("matvec", "env", "davidson"):
         L, R, W, x = rnd(chi, 5, chi), rnd(chi, 5, chi), rnd(5, 5, 2, 2), rnd(chi, 2, chi)
