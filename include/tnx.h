@@ -318,14 +318,24 @@ int tnx_gemm_df64(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, dou
 
 /* C = alpha * op(A) op(B) + beta * C, row-major FP64, on the tcgen05 tensor cores by exact
  * integer slicing (Ozaki scheme): rows of op(A) / columns of op(B) scaled by powers of two and
- * cut into eight 7-bit slices held exactly in BF16, the 36 slice products with s + t < 8
- * accumulated exactly in FP32 tensor memory over 128-long K chunks and summed in double-FP32.
- * Error ~2^-52 per product relative to max|row of op(A)| max|column of op(B)|. Returns
- * TNX_ERR_TIMEOUT if a bounded wait in the kernel expired (synchronises the stream). */
+ * cut into eight balanced base-128 digits held exactly in BF16, the 36 slice products with
+ * s + t < 8 accumulated exactly in FP32 tensor memory over 480-long K chunks and summed in
+ * double-FP32. Error ~2^-52 per product relative to max|row of op(A)| max|column of op(B)|.
+ * Returns TNX_ERR_TIMEOUT if a bounded wait in the kernel expired (synchronises the stream). */
 size_t tnx_gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k);
 int tnx_gemm_oz(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                 int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
                 void* workspace, size_t workspace_bytes, void* stream);
+/* The same product for `batch` operand sets at element strides sA, sB, sC (one launch; sets
+ * with mask[b] == 0 are skipped, mask may be null) and with K split into `nsplit` ranges whose
+ * partial products are added in range order (long-K products with small outputs: the QR's
+ * V^T C). Backs the tensor-core form of the lockstep chains' products and the gauge move's
+ * trailing updates. */
+size_t tnx_gemm_oz_batched_workspace_bytes(int64_t m, int64_t n, int64_t k, int batch, int nsplit);
+int tnx_gemm_oz_batched(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                        int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C,
+                        int64_t ldc, int64_t sC, int batch, int nsplit, const int* mask, void* workspace,
+                        size_t workspace_bytes, void* stream);
 
 /* C (m x n, row-major FP64) = A (m x k) B^T (B is n x k), both row-major FP64, computed as
  * three BF16 tensor-core products (split-BF16) with FP32 accumulation. Test / building-block

@@ -75,6 +75,9 @@ SIGNATURES = {
     "tnx_gemm_oz_workspace_bytes": (_sz, [_i64, _i64, _i64]),
     "tnx_gemm_oz": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _vp, _i64, _dbl, _vp, _i64, _vp, _sz,
                            _vp]),
+    "tnx_gemm_oz_batched_workspace_bytes": (_sz, [_i64, _i64, _i64, _int, _int]),
+    "tnx_gemm_oz_batched": (_int, [_int, _int, _i64, _i64, _i64, _dbl, _vp, _i64, _i64, _vp, _i64, _i64, _dbl, _vp,
+                                   _i64, _i64, _int, _int, _vp, _vp, _sz, _vp]),
     "tnx_gemm_bf16x3_workspace_bytes": (_sz, [_i64, _i64, _i64]),
     "tnx_gemm_bf16x3": (_int, [_i64, _i64, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tnx_tsdrg_block_hamiltonian": (_int, [_vp, _vp, _vp, _int, _vp, _vp, _int, _int, _vp]),

@@ -465,20 +465,47 @@ struct BDims {
 };
 
 // mask (device, B ints, may be null): chains whose entry is 0 are skipped by every launch
+// Batched FP64-class products: one tensor-core launch (Ozaki, every chain at its stride, masked
+// chains skipped) where scratch `oz` is given and the batch's product is large enough; the
+// strided-batched double-FP32 / FP64 GEMM otherwise.
+inline bool boz_applies(int64_t m, int64_t n, int64_t k, int B) {
+  return k >= 32 && m >= 32 && n >= 32 && double(m) * double(n) * double(k) * B >= double(1 << 26);
+}
+size_t boz_bytes(int64_t m, int64_t n, int64_t k, int B) {
+  return boz_applies(m, n, k, B) ? gemm_oz_ex_workspace_bytes(m, n, k, B, 1) : 0;
+}
+int bgemm(bool df, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+          int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C, int64_t ldc, int64_t sC,
+          int batch, cudaStream_t st, const int* mask, void* oz, size_t ozb) {
+  if (df && oz && boz_applies(m, n, k, batch) && ozb >= gemm_oz_ex_workspace_bytes(m, n, k, batch, 1))
+    return gemm_oz_ex(ta, tb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, 1, mask, oz, ozb, st);
+  return gemm_fp64_class(df, ta, tb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st, 0, mask);
+}
+// Ozaki scratch for the two products of a batched matvec / environment update of these shapes
+size_t bmatvec_oz_bytes(const BDims& g, int B) {
+  size_t b = boz_bytes(g.dl * g.chi_l, g.d * g.chi_r, g.chi_l, B);
+  auto mx = [&](size_t x) { b = x > b ? x : b; };
+  mx(boz_bytes(g.chi_l * g.d, g.chi_r, g.chi_r * g.dr, B));  // matvec, second product
+  mx(boz_bytes(g.chi_r * g.dr, g.chi_r, g.chi_l * g.d, B));  // rightward environment update
+  mx(boz_bytes(g.chi_l * g.d, g.dr * g.chi_r, g.chi_r, B));  // leftward environment update
+  mx(boz_bytes(g.chi_l * g.dl, g.chi_l, g.d * g.chi_r, B));
+  return b;
+}
+
 int bmatvec(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR, const double* x,
             int64_t sx, double* y, int64_t sy, int B, const BDims& g, double* T1, double* T2, bool df,
-            cudaStream_t st, const int* mask = nullptr) {
+            cudaStream_t st, const int* mask = nullptr, void* oz = nullptr, size_t ozb = 0) {
   const int64_t ne = g.ne();
   // T1[(w,a'),(s,c)] = sum_a L[a,(w,a')] x[a,(s,c)]
-  TNX_TRY(gemm_fp64_class(df, true, false, g.dl * g.chi_l, g.d * g.chi_r, g.chi_l, 1.0, L, g.dl * g.chi_l, sL, x,
-                          g.d * g.chi_r, sx, 0.0, T1, g.d * g.chi_r, ne, B, st, 0, mask));
+  TNX_TRY(bgemm(df, true, false, g.dl * g.chi_l, g.d * g.chi_r, g.chi_l, 1.0, L, g.dl * g.chi_l, sL, x,
+                g.d * g.chi_r, sx, 0.0, T1, g.d * g.chi_r, ne, B, st, mask, oz, ozb));
   const size_t smem = size_t(g.dl * g.dr * g.d * g.d) * sizeof(double);
   bw_left_kernel<<<dim3(bgrid(g.chi_l * g.chi_r, 128, 64), B), 128, smem, st>>>(
       T1, ne, W, sW, T2, ne, g.chi_l, int(g.d), g.chi_r, int(g.dl), int(g.dr), mask);
   TNX_LAUNCH_CHECK();
   // y[(a',s'),c'] = sum_{(c,v)} T2[(a',s'),(c,v)] R[(c,v),c']
-  TNX_TRY(gemm_fp64_class(df, false, false, g.chi_l * g.d, g.chi_r, g.chi_r * g.dr, 1.0, T2, g.chi_r * g.dr, ne, R,
-                          g.chi_r, sR, 0.0, y, g.chi_r, sy, B, st, 0, mask));
+  TNX_TRY(bgemm(df, false, false, g.chi_l * g.d, g.chi_r, g.chi_r * g.dr, 1.0, T2, g.chi_r * g.dr, ne, R, g.chi_r,
+                sR, 0.0, y, g.chi_r, sy, B, st, mask, oz, ozb));
   return TNX_OK;
 }
 
@@ -495,6 +522,8 @@ struct BDavWs {
   double *V, *AV, *x, *ax, *t, *diag, *Hm, *evals, *evecs, *evecs_prev, *h, *nrm2, *nrm2_0, *rn2, *T1, *T2, *xp,
       *axp;
   int *active, *count;
+  void* oz;
+  size_t oz_bytes;
 };
 
 size_t bdav_layout(const BDims& g, int B, int mb, void* base, BDavWs* w) {
@@ -511,6 +540,7 @@ size_t bdav_layout(const BDims& g, int B, int mb, void* base, BDavWs* w) {
          oevec = take(Bz * mb * 8), oh = take(Bz * mb * 8), on = take(Bz * 8), on0 = take(Bz * 8), orn = take(Bz * 8),
          oT1 = take(Bz * ne * 8), oT2 = take(Bz * ne * 8), oa = take(Bz * 4), oc = take(16),
          oep = take(Bz * mb * 8), oxp = take(Bz * n * 8), oaxp = take(Bz * n * 8);
+  const size_t ozb = bmatvec_oz_bytes(g, B), ooz = take(ozb);
   if (w && base) {
     char* p = static_cast<char*>(base);
     w->V = reinterpret_cast<double*>(p + oV);
@@ -533,6 +563,8 @@ size_t bdav_layout(const BDims& g, int B, int mb, void* base, BDavWs* w) {
     w->evecs_prev = reinterpret_cast<double*>(p + oep);
     w->xp = reinterpret_cast<double*>(p + oxp);
     w->axp = reinterpret_cast<double*>(p + oaxp);
+    w->oz = ozb ? p + ooz : nullptr;
+    w->oz_bytes = ozb;
   }
   return off;
 }
@@ -547,7 +579,7 @@ extern "C" {
 size_t tnx_batched_matvec1_workspace_bytes(int64_t chi_l, int64_t d, int64_t chi_r, int64_t dl, int64_t dr,
                                            int batch) {
   const BDims g{chi_l, d, chi_r, dl, dr};
-  return 2 * align_up(size_t(batch) * size_t(g.ne()) * 8);
+  return 2 * align_up(size_t(batch) * size_t(g.ne()) * 8) + align_up(bmatvec_oz_bytes(g, batch));
 }
 
 int tnx_batched_matvec1(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR,
@@ -565,7 +597,10 @@ int tnx_batched_matvec1(const double* L, int64_t sL, const double* W, int64_t sW
   }
   double* T1 = static_cast<double*>(workspace);
   double* T2 = reinterpret_cast<double*>(static_cast<char*>(workspace) + align_up(size_t(batch) * g.ne() * 8));
-  return bmatvec(L, sL, W, sW, R, sR, x, sx, y, sy, batch, g, T1, T2, use_df64(precision), as_stream(stream));
+  const size_t ozb = bmatvec_oz_bytes(g, batch);
+  void* oz = ozb ? static_cast<char*>(workspace) + 2 * align_up(size_t(batch) * g.ne() * 8) : nullptr;
+  return bmatvec(L, sL, W, sW, R, sR, x, sx, y, sy, batch, g, T1, T2, use_df64(precision), as_stream(stream), nullptr,
+                 oz, ozb);
 }
 
 int tnx_batched_full_matrix1(const double* L, int64_t sL, const double* W, int64_t sW, const double* R, int64_t sR,
@@ -603,23 +638,25 @@ int tnx_batched_env_update(int direction, const double* E_in, int64_t sE, const 
   const int64_t ne = g.ne();
   double* T1 = static_cast<double*>(workspace);
   double* T2 = reinterpret_cast<double*>(static_cast<char*>(workspace) + align_up(size_t(batch) * ne * 8));
+  const size_t ozb = bmatvec_oz_bytes(g, batch);
+  void* oz = ozb ? static_cast<char*>(workspace) + 2 * align_up(size_t(batch) * ne * 8) : nullptr;
   const size_t smem = size_t(dl * dr * d * d) * sizeof(double);
   if (direction == 1) {
-    TNX_TRY(gemm_fp64_class(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, E_in, dl * chi_l, sE, A, d * chi_r,
-                            sA, 0.0, T1, d * chi_r, ne, batch, st));
+    TNX_TRY(bgemm(df, true, false, dl * chi_l, d * chi_r, chi_l, 1.0, E_in, dl * chi_l, sE, A, d * chi_r, sA, 0.0, T1,
+                  d * chi_r, ne, batch, st, nullptr, oz, ozb));
     bw_left_kernel<<<dim3(bgrid(chi_l * chi_r, 128, 64), batch), 128, smem, st>>>(T1, ne, W, sW, T2, ne, chi_l,
                                                                                   int(d), chi_r, int(dl), int(dr));
     TNX_LAUNCH_CHECK();
-    TNX_TRY(gemm_fp64_class(df, true, false, chi_r * dr, chi_r, chi_l * d, 1.0, T2, chi_r * dr, ne, A, chi_r, sA,
-                            0.0, E_out, chi_r, sO, batch, st));
+    TNX_TRY(bgemm(df, true, false, chi_r * dr, chi_r, chi_l * d, 1.0, T2, chi_r * dr, ne, A, chi_r, sA, 0.0, E_out,
+                  chi_r, sO, batch, st, nullptr, oz, ozb));
   } else {
-    TNX_TRY(gemm_fp64_class(df, false, false, chi_l * d, dr * chi_r, chi_r, 1.0, A, chi_r, sA, E_in, dr * chi_r, sE,
-                            0.0, T1, dr * chi_r, ne, batch, st));
+    TNX_TRY(bgemm(df, false, false, chi_l * d, dr * chi_r, chi_r, 1.0, A, chi_r, sA, E_in, dr * chi_r, sE, 0.0, T1,
+                  dr * chi_r, ne, batch, st, nullptr, oz, ozb));
     bw_right_kernel<<<dim3(bgrid(chi_l * chi_r, 128, 64), batch), 128, smem, st>>>(T1, ne, W, sW, T2, ne, chi_l,
                                                                                    int(d), chi_r, int(dl), int(dr));
     TNX_LAUNCH_CHECK();
-    TNX_TRY(gemm_fp64_class(df, false, true, chi_l * dl, chi_l, d * chi_r, 1.0, T2, d * chi_r, ne, A, d * chi_r, sA,
-                            0.0, E_out, chi_l, sO, batch, st));
+    TNX_TRY(bgemm(df, false, true, chi_l * dl, chi_l, d * chi_r, 1.0, T2, d * chi_r, ne, A, d * chi_r, sA, 0.0, E_out,
+                  chi_l, sO, batch, st, nullptr, oz, ozb));
   }
   return TNX_OK;
 }
@@ -691,7 +728,7 @@ int tnx_batched_davidson1(const double* L, int64_t sL, const double* W, int64_t 
     TNX_LAUNCH_CHECK();
     double* avk = w.AV + int64_t(k) * n;
     // converged chains are masked out of the products too
-    TNX_TRY(bmatvec(L, sL, W, sW, R, sR, vk, sVB, avk, sVB, B, g, w.T1, w.T2, df, st, w.active));
+    TNX_TRY(bmatvec(L, sL, W, sW, R, sR, vk, sVB, avk, sVB, B, g, w.T1, w.T2, df, st, w.active, w.oz, w.oz_bytes));
     // column k of the projected matrix (and its mirror row)
     bdots_kernel<<<dim3(k + 1, B), BT, 0, st>>>(w.V, sVB, n, avk, sVB, w.Hm + k, int64_t(mb) * mb, mb,
                                                 w.Hm + int64_t(k) * mb, 1, w.active);
@@ -747,7 +784,9 @@ size_t tnx_batched_gauge_move_workspace_bytes(int direction, int64_t chi_l, int6
                                               int64_t chi_other, int batch) {
   const int64_t nb = direction == 1 ? chi_r : chi_l;
   const int64_t other = direction == 1 ? chi_r * d * chi_other : chi_other * d * chi_l;
-  return align_up(size_t(batch) * nb * nb * 8) + align_up(size_t(batch) * other * 8);
+  const size_t ozb = direction == 1 ? boz_bytes(chi_r, d * chi_other, chi_r, batch)
+                                    : boz_bytes(chi_other * d, chi_l, chi_l, batch);
+  return align_up(size_t(batch) * nb * nb * 8) + align_up(size_t(batch) * other * 8) + align_up(ozb);
 }
 
 int tnx_batched_gauge_move(int direction, double* A_site, int64_t sA, double* A_nb, int64_t sN, int batch,
@@ -777,14 +816,17 @@ int tnx_batched_gauge_move(int direction, double* A_site, int64_t sA, double* A_
   TNX_LAUNCH_CHECK();
   const bool df = use_df64(precision);
   const int64_t other = direction == 1 ? chi_r * d * chi_other : chi_other * d * chi_l;
+  const size_t ozb = direction == 1 ? boz_bytes(chi_r, d * chi_other, chi_r, batch)
+                                    : boz_bytes(chi_other * d, chi_l, chi_l, batch);
+  void* oz = ozb ? reinterpret_cast<char*>(tmp) + align_up(size_t(batch) * other * 8) : nullptr;
   if (direction == 1) {
     // A_next (chi_r x (d chi_other)) <- R A_next
-    TNX_TRY(gemm_fp64_class(df, false, false, chi_r, d * chi_other, chi_r, 1.0, Rm, chi_r, chi_r * chi_r, A_nb,
-                            d * chi_other, sN, 0.0, tmp, d * chi_other, other, batch, st));
+    TNX_TRY(bgemm(df, false, false, chi_r, d * chi_other, chi_r, 1.0, Rm, chi_r, chi_r * chi_r, A_nb, d * chi_other,
+                  sN, 0.0, tmp, d * chi_other, other, batch, st, nullptr, oz, ozb));
   } else {
     // A_prev ((chi_other d) x chi_l) <- A_prev R^T
-    TNX_TRY(gemm_fp64_class(df, false, true, chi_other * d, chi_l, chi_l, 1.0, A_nb, chi_l, sN, Rm, chi_l,
-                            chi_l * chi_l, 0.0, tmp, chi_l, other, batch, st));
+    TNX_TRY(bgemm(df, false, true, chi_other * d, chi_l, chi_l, 1.0, A_nb, chi_l, sN, Rm, chi_l, chi_l * chi_l, 0.0,
+                  tmp, chi_l, other, batch, st, nullptr, oz, ozb));
   }
   bcopy_kernel<<<dim3(bgrid(other, 256, 16), batch), 256, 0, st>>>(tmp, other, A_nb, sN, other, nullptr);
   TNX_LAUNCH_CHECK();

@@ -28,6 +28,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "tc_ptx.cuh"
@@ -53,8 +54,11 @@ constexpr uint32_t OZ_TMEM_COLS = 512;
 // a row with Inf or NaN, whose outputs the GEMM epilogue sets to NaN.
 constexpr int OZ_SCAN_K = 256;
 __global__ void oz_rowmax_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
-                                 int* __restrict__ bmax) {
+                                 int* __restrict__ bmax, int64_t s_src, int64_t s_bmax, const int* __restrict__ mask) {
   __shared__ int tile[32][33];
+  if (mask && !mask[blockIdx.z]) return;  // a chain the caller masked out
+  src += int64_t(blockIdx.z) * s_src;
+  bmax += int64_t(blockIdx.z) * s_bmax;
   const int64_t r0 = int64_t(blockIdx.y) * 32, kb = int64_t(blockIdx.x) * OZ_SCAN_K;
   const int tx = threadIdx.x, ty = threadIdx.y;
   int best = 0;  // biased exponent, 0 = zero / denormal
@@ -89,8 +93,12 @@ __device__ __forceinline__ uint16_t bf16_of_small_int(unsigned q, unsigned sign)
 // zero for r >= rows or k >= K.
 __global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
                                 const int* __restrict__ exps, uint16_t* __restrict__ planes, int64_t rows_pad,
-                                int64_t Kp) {
+                                int64_t Kp, int64_t s_src, const int* __restrict__ mask) {
   __shared__ double tile[32][33];
+  if (mask && !mask[blockIdx.z]) return;
+  src += int64_t(blockIdx.z) * s_src;
+  exps += int64_t(blockIdx.z) * rows_pad;
+  planes += int64_t(blockIdx.z) * OZ_S * rows_pad * Kp;
   const int64_t r0 = int64_t(blockIdx.y) * 32, k0 = int64_t(blockIdx.x) * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int i = ty; i < 32; i += 8) {
@@ -128,22 +136,35 @@ __global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, in
 // Stage layout (one K block of 32): A slices 0..S-1 (128 x 32 bf16, 8 KB each), then B slices
 // 0..S-1 (64 x 32 bf16, 4 KB each), 64-byte swizzle; every slice tile is loaded once per K
 // block and feeds all S(S+1)/2 slice products that use it.
+// Batch and split-K: blockIdx.z = bz * nsplit + sz. Chain bz reads its slice planes at plane rows
+// (bz * S + q) * Mp (A) / (bz * S + q) * Np (B) and its exponents at ea + bz Mp / eb + bz Np;
+// split sz covers K blocks [sz kbs, (sz + 1) kbs). With nsplit == 1 the CTA writes
+// C + bz sC = alpha P + beta C; otherwise the unscaled partial P to part[(sz * batch + bz) M N]
+// (row-major, ld N), which oz_split_reduce_kernel sums in split order.
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     oz_gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int M, int N,
                    int Kp, int Mp, int Np, const int* __restrict__ ea, const int* __restrict__ eb, double alpha,
-                   double beta, double* __restrict__ C, int64_t ldc, int* __restrict__ err_flag) {
+                   double beta, double* __restrict__ C, int64_t ldc, int* __restrict__ err_flag, int batch,
+                   int nsplit, int kbs, int64_t sC, double* __restrict__ part, const int* __restrict__ mask) {
   constexpr uint32_t A_TILE = OZ_BM * OZ_BK * 2, B_TILE = OZ_BN * OZ_BK * 2;
   constexpr uint32_t STAGE_BYTES = OZ_S * (A_TILE + B_TILE);
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[OZ_STAGES], empty_bar[OZ_STAGES], chunk_full, chunk_empty;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
+  const int bz = int(blockIdx.z) / nsplit, sz = int(blockIdx.z) % nsplit;
+  if (mask && !mask[bz]) return;  // uniform over the CTA, before any barrier or TMEM allocation
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const int m0 = blockIdx.y * OZ_BM, n0 = blockIdx.x * OZ_BN;
-  const int kblocks = Kp / OZ_BK;
+  const int kb_all = Kp / OZ_BK;
+  const int kb0 = sz * kbs, kb1 = min(kb_all, kb0 + kbs);
+  const int kblocks = kb1 > kb0 ? kb1 - kb0 : 0;
   const int kb_per_chunk = OZ_KC / OZ_BK;
   const int nchunks = (kblocks + kb_per_chunk - 1) / kb_per_chunk;
+  const int a_row0 = bz * OZ_S * Mp, b_row0 = bz * OZ_S * Np;
+  ea += int64_t(bz) * Mp;
+  eb += int64_t(bz) * Np;
 
   if (threadIdx.x == 0) {
     for (int st = 0; st < OZ_STAGES; ++st) {
@@ -182,8 +203,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const uint32_t fb = smem_u32(&full_bar[st]);
         mbar_expect_tx(fb, STAGE_BYTES);
         for (int q = 0; q < OZ_S; ++q) {
-          tma_load_2d(sa + q * A_TILE, &ta, fb, kb * OZ_BK, q * Mp + m0);
-          tma_load_2d(sb + q * B_TILE, &tb, fb, kb * OZ_BK, q * Np + n0);
+          tma_load_2d(sa + q * A_TILE, &ta, fb, (kb0 + kb) * OZ_BK, a_row0 + q * Mp + m0);
+          tma_load_2d(sb + q * B_TILE, &tb, fb, (kb0 + kb) * OZ_BK, b_row0 + q * Np + n0);
         }
         ++issued;
       }
@@ -272,15 +293,27 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (ok && row < M) {
       const int er = row_scale_exp(ea[row]);
       const bool row_nonfinite = ea[row] == 2047;  // the row holds Inf / NaN: its slices are not the value
-      double* o = C + int64_t(row) * ldc + n0;
+      if (nsplit == 1) {
+        double* o = C + int64_t(bz) * sC + int64_t(row) * ldc + n0;
 #pragma unroll
-      for (int j = 0; j < OZ_BN; ++j) {
-        if (n0 + j < N) {
-          double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
-          if (row_nonfinite || eb[n0 + j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
-          v *= alpha;
-          if (beta != 0.0) v = fma(beta, o[j], v);
-          o[j] = v;
+        for (int j = 0; j < OZ_BN; ++j) {
+          if (n0 + j < N) {
+            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
+            if (row_nonfinite || eb[n0 + j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
+            v *= alpha;
+            if (beta != 0.0) v = fma(beta, o[j], v);
+            o[j] = v;
+          }
+        }
+      } else {
+        double* o = part + (int64_t(sz) * batch + bz) * M * N + int64_t(row) * N + n0;
+#pragma unroll
+        for (int j = 0; j < OZ_BN; ++j) {
+          if (n0 + j < N) {
+            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
+            if (row_nonfinite || eb[n0 + j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
+            o[j] = v;
+          }
         }
       }
     }
@@ -293,21 +326,40 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   }
 }
 
+// C[bz] = alpha sum_s part[s][bz] + beta C[bz] (split order fixed: deterministic)
+__global__ void oz_split_reduce_kernel(const double* __restrict__ part, int nsplit, int batch, int M, int N,
+                                       double alpha, double beta, double* __restrict__ C, int64_t ldc, int64_t sC,
+                                       const int* __restrict__ mask) {
+  const int bz = blockIdx.y;
+  if (mask && !mask[bz]) return;
+  const int64_t MN = int64_t(M) * N;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < MN; e += int64_t(gridDim.x) * blockDim.x) {
+    double v = 0.0;
+    for (int s = 0; s < nsplit; ++s) v += part[(int64_t(s) * batch + bz) * MN + e];
+    double* o = C + int64_t(bz) * sC + (e / N) * ldc + (e % N);
+    v *= alpha;
+    if (beta != 0.0) v = fma(beta, *o, v);
+    *o = v;
+  }
+}
+
 struct OzLayout {
   int64_t Mp, Np, Kp;
   uint16_t *sa, *sb;
   int *ea, *eb, *flag;
+  double* part;
 };
 
-size_t oz_layout(int64_t m, int64_t n, int64_t k, void* base, OzLayout* L) {
+size_t oz_layout(int64_t m, int64_t n, int64_t k, int64_t batch, int nsplit, void* base, OzLayout* L) {
   OzLayout o;
   o.Mp = (m + OZ_BM - 1) / OZ_BM * OZ_BM;
   o.Np = (n + OZ_BN - 1) / OZ_BN * OZ_BN;
   o.Kp = (k + OZ_BK - 1) / OZ_BK * OZ_BK;
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t r = off; off += align_up(bytes); return r; };
-  const size_t osa = take(size_t(OZ_S) * o.Mp * o.Kp * 2), osb = take(size_t(OZ_S) * o.Np * o.Kp * 2),
-               oea = take(size_t(o.Mp) * 4), oeb = take(size_t(o.Np) * 4), ofl = take(4);
+  const size_t osa = take(size_t(batch) * OZ_S * o.Mp * o.Kp * 2), osb = take(size_t(batch) * OZ_S * o.Np * o.Kp * 2),
+               oea = take(size_t(batch) * o.Mp * 4), oeb = take(size_t(batch) * o.Np * 4), ofl = take(4),
+               opt = take(nsplit > 1 ? size_t(nsplit) * batch * m * n * 8 : 0);
   if (base && L) {
     char* b = static_cast<char*>(base);
     o.sa = reinterpret_cast<uint16_t*>(b + osa);
@@ -315,6 +367,7 @@ size_t oz_layout(int64_t m, int64_t n, int64_t k, void* base, OzLayout* L) {
     o.ea = reinterpret_cast<int*>(b + oea);
     o.eb = reinterpret_cast<int*>(b + oeb);
     o.flag = reinterpret_cast<int*>(b + ofl);
+    o.part = reinterpret_cast<double*>(b + opt);
     *L = o;
   }
   return off;
@@ -324,16 +377,26 @@ size_t oz_smem_bytes() { return size_t(OZ_STAGES) * OZ_S * (OZ_BM * OZ_BK * 2 + 
 
 }  // namespace
 
-size_t gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k) { return oz_layout(m, n, k, nullptr, nullptr); }
+size_t gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k) { return oz_layout(m, n, k, 1, 1, nullptr, nullptr); }
+size_t gemm_oz_ex_workspace_bytes(int64_t m, int64_t n, int64_t k, int batch, int nsplit) {
+  return oz_layout(m, n, k, batch, nsplit, nullptr, nullptr);
+}
 
-int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
-            const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws, size_t ws_bytes,
-            cudaStream_t st) {
-  if (m <= 0 || n <= 0) return TNX_OK;
-  if (k <= 0) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
-  TNX_CHECK_SHAPE(m <= (int64_t(1) << 30) / OZ_S && n <= (int64_t(1) << 30) / OZ_S, "gemm_oz: operand too large");
+int gemm_oz_ex(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+               int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C, int64_t ldc, int64_t sC,
+               int batch, int nsplit, const int* mask, void* ws, size_t ws_bytes, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || batch <= 0) return TNX_OK;
+  TNX_CHECK_ARG(nsplit >= 1 && batch <= 65535 && int64_t(batch) * nsplit <= 65535, "gemm_oz: batch %d x split %d",
+                batch, nsplit);
+  if (k <= 0) {
+    if (batch == 1 && !mask) return gemm_f64(ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+    return gemm_f64(ta, tb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st, 0, mask);
+  }
+  TNX_CHECK_SHAPE(int64_t(batch) * OZ_S * ((m + OZ_BM - 1) / OZ_BM * OZ_BM) < (int64_t(1) << 31) &&
+                      int64_t(batch) * OZ_S * ((n + OZ_BN - 1) / OZ_BN * OZ_BN) < (int64_t(1) << 31),
+                  "gemm_oz: operand too large");
   OzLayout L;
-  const size_t need = oz_layout(m, n, k, ws, &L);
+  const size_t need = oz_layout(m, n, k, batch, nsplit, ws, &L);
   if (!ws || ws_bytes < need) {
     set_error("gemm_oz: workspace %zu bytes < required %zu", ws_bytes, need);
     return TNX_ERR_WORKSPACE;
@@ -344,39 +407,56 @@ int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, con
   dim3 tb2(32, 8);
   // row maxima (atomicMax into zeroed arrays) and the error flag: ea, eb and flag are consecutive
   TNX_CUDA(cudaMemsetAsync(L.ea, 0, reinterpret_cast<char*>(L.flag + 1) - reinterpret_cast<char*>(L.ea), st));
-  const unsigned kscan = unsigned((k + OZ_SCAN_K - 1) / OZ_SCAN_K);
-  oz_rowmax_kernel<<<dim3(kscan, unsigned(L.Mp / 32)), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea);
+  const unsigned kscan = unsigned((k + OZ_SCAN_K - 1) / OZ_SCAN_K), bzs = unsigned(batch);
+  oz_rowmax_kernel<<<dim3(kscan, unsigned(L.Mp / 32), bzs), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea, sA, L.Mp, mask);
   TNX_LAUNCH_CHECK();
-  oz_rowmax_kernel<<<dim3(kscan, unsigned(L.Np / 32)), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb);
+  oz_rowmax_kernel<<<dim3(kscan, unsigned(L.Np / 32), bzs), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb, sB, L.Np, mask);
   TNX_LAUNCH_CHECK();
-  oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Mp / 32)), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea, L.sa,
-                                                                                  L.Mp, L.Kp);
+  oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Mp / 32), bzs), tb2, 0, st>>>(A, m, k, a_rs, a_ks, L.ea,
+                                                                                        L.sa, L.Mp, L.Kp, sA, mask);
   TNX_LAUNCH_CHECK();
-  oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Np / 32)), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb, L.sb,
-                                                                                  L.Np, L.Kp);
+  oz_slice_kernel<<<dim3(unsigned(L.Kp / 32), unsigned(L.Np / 32), bzs), tb2, 0, st>>>(B, n, k, b_rs, b_ks, L.eb,
+                                                                                        L.sb, L.Np, L.Kp, sB, mask);
   TNX_LAUNCH_CHECK();
   CUtensorMap ma, mb;
-  TNX_TRY(make_tma_map_bf16(&ma, L.sa, int64_t(OZ_S) * L.Mp, L.Kp, OZ_BK, OZ_BM));
-  TNX_TRY(make_tma_map_bf16(&mb, L.sb, int64_t(OZ_S) * L.Np, L.Kp, OZ_BK, OZ_BN));
+  TNX_TRY(make_tma_map_bf16(&ma, L.sa, int64_t(batch) * OZ_S * L.Mp, L.Kp, OZ_BK, OZ_BM));
+  TNX_TRY(make_tma_map_bf16(&mb, L.sb, int64_t(batch) * OZ_S * L.Np, L.Kp, OZ_BK, OZ_BN));
   const size_t smem = oz_smem_bytes();
   static std::atomic<bool> attr{false};  // idempotent setup; threads may race to it
   if (!attr.load()) {
     TNX_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     attr.store(true);
   }
-  dim3 grid(unsigned(L.Np / OZ_BN), unsigned(L.Mp / OZ_BM));
+  const int kb_all = int(L.Kp / OZ_BK);
+  const int kbs = (kb_all + nsplit - 1) / nsplit;
+  nsplit = (kb_all + kbs - 1) / kbs;  // no empty splits
+  dim3 grid(unsigned(L.Np / OZ_BN), unsigned(L.Mp / OZ_BM), unsigned(batch * nsplit));
   profile_mark(KF_OZ_GEMM, st, true);
   oz_gemm_kernel<<<grid, OZ_THREADS, smem, st>>>(ma, mb, int(m), int(n), int(L.Kp), int(L.Mp), int(L.Np), L.ea, L.eb,
-                                                 alpha, beta, C, ldc, L.flag);
-  profile_mark(KF_OZ_GEMM, st, false);
-  profile_work(KF_OZ_GEMM, 2.0 * double(m) * n * k, 8.0 * (double(m) * k + double(k) * n + double(m) * n));
+                                                 alpha, beta, C, ldc, L.flag, batch, nsplit, kbs, sC, L.part, mask);
   TNX_LAUNCH_CHECK();
+  if (nsplit > 1) {
+    const int64_t mn = m * n;
+    const unsigned gx = unsigned(std::min<int64_t>((mn + 255) / 256, 64));
+    oz_split_reduce_kernel<<<dim3(gx, unsigned(batch)), 256, 0, st>>>(L.part, nsplit, batch, int(m), int(n), alpha,
+                                                                      beta, C, ldc, sC, mask);
+    TNX_LAUNCH_CHECK();
+  }
+  profile_mark(KF_OZ_GEMM, st, false);
+  profile_work(KF_OZ_GEMM, 2.0 * double(m) * n * k * batch,
+               8.0 * batch * (double(m) * k + double(k) * n + double(m) * n));
   return TNX_OK;
+}
+
+int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+            const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws, size_t ws_bytes,
+            cudaStream_t st) {
+  return gemm_oz_ex(ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, 1, nullptr, ws, ws_bytes, st);
 }
 
 int gemm_oz_flag(void* ws, int64_t m, int64_t n, int64_t k, int** flag) {
   OzLayout L;
-  oz_layout(m, n, k, ws, &L);
+  oz_layout(m, n, k, 1, 1, ws, &L);
   *flag = L.flag;
   return TNX_OK;
 }
@@ -405,6 +485,33 @@ int tnx_gemm_oz(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, doubl
   TNX_CUDA(cudaStreamSynchronize(st));
   if (h) {
     set_error("tnx_gemm_oz: a bounded wait in the tensor-core kernel expired");
+    return TNX_ERR_TIMEOUT;
+  }
+  return TNX_OK;
+}
+
+size_t tnx_gemm_oz_batched_workspace_bytes(int64_t m, int64_t n, int64_t k, int batch, int nsplit) {
+  return gemm_oz_ex_workspace_bytes(m, n, k, batch < 1 ? 1 : batch, nsplit < 1 ? 1 : nsplit);
+}
+
+int tnx_gemm_oz_batched(int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                        int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C,
+                        int64_t ldc, int64_t sC, int batch, int nsplit, const int* mask, void* workspace,
+                        size_t workspace_bytes, void* stream) {
+  TNX_CHECK_ARG(A && B && C, "null pointer");
+  TNX_CHECK_ARG(m >= 0 && n >= 0 && k >= 0 && batch >= 1 && nsplit >= 1, "negative size, batch or split");
+  cudaStream_t st = as_stream(stream);
+  TNX_TRY(gemm_oz_ex(trans_a != 0, trans_b != 0, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch,
+                     nsplit, mask, workspace, workspace_bytes, st));
+  int* flag = nullptr;
+  OzLayout L;
+  oz_layout(m, n, k, batch, nsplit, workspace, &L);
+  flag = L.flag;
+  int h = 0;
+  TNX_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  TNX_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("tnx_gemm_oz_batched: a bounded wait in the tensor-core kernel expired");
     return TNX_ERR_TIMEOUT;
   }
   return TNX_OK;

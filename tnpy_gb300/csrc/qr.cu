@@ -19,6 +19,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <mutex>
 #include <string>
@@ -784,17 +785,36 @@ int apply_panel_narrow(int64_t m, int64_t mp, int nb, int NB, const double* Vp, 
 
 // C -= V T^T V^T C for the mp x nc column-major block C (ld m): the trailing update of one
 // panel (V: mp x nb column-major in Vp, T: column-major ld NB)
+// With `oz` (FP64-class modes, large trailing blocks) the two large products run on the Ozaki
+// GEMM: V^T C split over K (QR_OZ_SPLIT ranges), C^T -= W2^T V^T with K = nb.
+constexpr int QR_OZ_SPLIT = 16;
+inline bool bulk_on_oz(int64_t mp, int64_t nc) { return mp >= 256 && nc >= 128; }
+size_t bulk_oz_bytes(int64_t m, int64_t n) {
+  return std::max(gemm_oz_ex_workspace_bytes(QBMAX, n, m, 1, QR_OZ_SPLIT), gemm_oz_ex_workspace_bytes(n, m, QBMAX, 1, 1));
+}
+
 int apply_panel_t(int64_t m, int64_t mp, int nb, int NB, const double* Vp, const double* Tp, double* C, int64_t nc,
-                  double* W1, double* W2, double* part, int64_t part_cap, cudaStream_t st, bool df) {
+                  double* W1, double* W2, double* part, int64_t part_cap, cudaStream_t st, bool df,
+                  void* oz = nullptr, size_t ozb = 0) {
   if (nc <= 0) return TNX_OK;
+  const bool on_oz = df && oz && bulk_on_oz(mp, nc);
   // Row-major views: C (column-major mp x nc, ld m) is C^T (nc x mp, ld m), V is V^T (nb x mp).
   // W1 (nb x nc) = V^T C  (short output rows, long K: split over K; finer for narrow C)
-  const int ns = nc <= NB ? qr_nsplit_cap(mp, nb, nc, part_cap) : qr_nsplit(mp);
-  TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, Vp, mp, C, m, 0.0, W1, nc, ns, part, st, df));
+  if (on_oz) {
+    TNX_TRY(gemm_oz_ex(false, true, nb, nc, mp, 1.0, Vp, mp, 0, C, m, 0, 0.0, W1, nc, 0, 1, QR_OZ_SPLIT, nullptr, oz,
+                       ozb, st));
+  } else {
+    const int ns = nc <= NB ? qr_nsplit_cap(mp, nb, nc, part_cap) : qr_nsplit(mp);
+    TNX_TRY(gemm_f64_splitk(false, true, nb, nc, mp, 1.0, Vp, mp, C, m, 0.0, W1, nc, ns, part, st, df));
+  }
   // W2 = T^T W1   (T column-major with ld NB is T^T row-major)
   TNX_TRY(gemm_fp64_class(df, false, false, nb, nc, nb, 1.0, Tp, NB, 0, W1, nc, 0, 0.0, W2, nc, 0, 1, st));
   // C -= V W2, i.e. C^T -= W2^T V^T
-  TNX_TRY(gemm_fp64_class(df, true, false, nc, mp, nb, -1.0, W2, nc, 0, Vp, mp, 0, 1.0, C, m, 0, 1, st));
+  if (on_oz) {
+    TNX_TRY(gemm_oz_ex(true, false, nc, mp, nb, -1.0, W2, nc, 0, Vp, mp, 0, 1.0, C, m, 0, 1, 1, nullptr, oz, ozb, st));
+  } else {
+    TNX_TRY(gemm_fp64_class(df, true, false, nc, mp, nb, -1.0, W2, nc, 0, Vp, mp, 0, 1.0, C, m, 0, 1, st));
+  }
   return TNX_OK;
 }
 
@@ -847,8 +867,10 @@ int look_ahead(LookAhead** out) {
 struct WyWs {
   double *V, *S, *Tf, *X, *Y;  // S: the n x 64 block V^T V_p of the current step, Y: S T_p
   double* part;                // split-K scratch of the V^T V_p products
-  void* oz;
+  void* oz;                    // Ozaki scratch of the WY stream (and of X and Q after it)
   size_t oz_bytes;
+  void* oz_bulk;               // Ozaki scratch of the bulk trailing updates (look-ahead stream)
+  size_t oz_bulk_bytes;
 };
 
 inline bool wy_applies(int64_t m, int64_t n, bool df) { return df && use_oz(n, n, m) && n >= 256; }
@@ -856,6 +878,8 @@ inline bool wy_applies(int64_t m, int64_t n, bool df) { return df && use_oz(n, n
 size_t wy_oz_bytes(int64_t m, int64_t n) {
   size_t b = gemm_oz_workspace_bytes(n, n, n);  // X
   auto mx = [&](size_t x) { b = x > b ? x : b; };
+  mx(gemm_oz_ex_workspace_bytes(n, QBMAX, m, 1, QR_OZ_SPLIT));  // V[:, 0:j0]^T V_p
+  mx(gemm_oz_ex_workspace_bytes(n, QBMAX, n, 1, QR_OZ_SPLIT));  // Tf Y
   mx(gemm_oz_workspace_bytes(m, n, n));  // Q, row-major output
   mx(gemm_oz_workspace_bytes(n, m, n));  // Q, column-major output
   return b;
@@ -866,7 +890,8 @@ size_t wy_layout(int64_t m, int64_t n, void* base, WyWs* w) {
   auto take = [&](size_t bytes) { size_t o = off; off += align_up(bytes); return o; };
   const size_t oV = take(size_t(m) * n * 8), oS = take(size_t(n) * n * 8), oT = take(size_t(n) * n * 8),
                oX = take(size_t(n) * n * 8), oY = take(size_t(n) * n * 8 / 4),
-               oP = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8), obz = wy_oz_bytes(m, n), oZ = take(obz);
+               oP = take(size_t(QR_SPLIT_MAX) * n * QBMAX * 8), obz = wy_oz_bytes(m, n), oZ = take(obz),
+               obb = bulk_oz_bytes(m, n), oB = take(obb);
   if (w && base) {
     char* b = static_cast<char*>(base);
     w->V = reinterpret_cast<double*>(b + oV);
@@ -877,6 +902,8 @@ size_t wy_layout(int64_t m, int64_t n, void* base, WyWs* w) {
     w->part = reinterpret_cast<double*>(b + oP);
     w->oz = b + oZ;
     w->oz_bytes = obz;
+    w->oz_bulk = b + oB;
+    w->oz_bulk_bytes = obb;
   }
   return off;
 }
@@ -911,13 +938,24 @@ int wy_append_panel(int64_t m, int64_t n, int NB, int64_t j0, int nb, const doub
   // S (j0 x nb, ld nb) = V[:, 0:j0]^T V_p over rows >= j0, where V_p is nonzero
   // (op(A)(i, k) = V(j0 + k, i); op(B)(k, j) = V(j0 + k, j0 + j))
   const int64_t K = m - j0;
-  TNX_TRY(gemm_f64_splitk(false, true, j0, nb, K, 1.0, y.V + j0, m, y.V + j0 * m + j0, m, 0.0, y.S, nb,
-                          qr_nsplit_cap(K, j0, nb, int64_t(QR_SPLIT_MAX) * n * QBMAX), part, st, true));
+  const bool on_oz = j0 >= 256;
+  if (on_oz) {
+    TNX_TRY(gemm_oz_ex(false, true, j0, nb, K, 1.0, y.V + j0, m, 0, y.V + j0 * m + j0, m, 0, 0.0, y.S, nb, 0, 1,
+                       QR_OZ_SPLIT, nullptr, y.oz, y.oz_bytes, st));
+  } else {
+    TNX_TRY(gemm_f64_splitk(false, true, j0, nb, K, 1.0, y.V + j0, m, y.V + j0 * m + j0, m, 0.0, y.S, nb,
+                            qr_nsplit_cap(K, j0, nb, int64_t(QR_SPLIT_MAX) * n * QBMAX), part, st, true));
+  }
   // Y (j0 x nb, ld nb) = S T_p   (op(B)(k, j) = T_p(k, j) = Tp[j NB + k])
   TNX_TRY(gemm_fp64_class(true, false, true, j0, nb, nb, 1.0, y.S, nb, 0, Tp, NB, 0, 0.0, y.Y, nb, 0, 1, st));
   // Tf[0:j0, j0:j0+nb] = -Tf[0:j0, 0:j0] Y  (K = j0 long, nb = 64 wide: split over K)
-  TNX_TRY(gemm_f64_splitk(false, false, j0, nb, j0, -1.0, y.Tf, n, y.Y, nb, 0.0, y.Tf + j0, n,
-                          qr_nsplit_cap(j0, j0, nb, int64_t(QR_SPLIT_MAX) * n * QBMAX), y.part, st, true));
+  if (on_oz) {
+    TNX_TRY(gemm_oz_ex(false, false, j0, nb, j0, -1.0, y.Tf, n, 0, y.Y, nb, 0, 0.0, y.Tf + j0, n, 0, 1, QR_OZ_SPLIT,
+                       nullptr, y.oz, y.oz_bytes, st));
+  } else {
+    TNX_TRY(gemm_f64_splitk(false, false, j0, nb, j0, -1.0, y.Tf, n, y.Y, nb, 0.0, y.Tf + j0, n,
+                            qr_nsplit_cap(j0, j0, nb, int64_t(QR_SPLIT_MAX) * n * QBMAX), y.part, st, true));
+  }
   return TNX_OK;
 }
 
@@ -963,7 +1001,7 @@ int qr_colmajor(int64_t m, int64_t n, QrWs& w, cudaStream_t st, bool df = false,
     if (rest > 0) {
       TNX_CUDA(cudaStreamWaitEvent(la->aux, la->ev_v, 0));
       TNX_TRY(apply_panel_t(m, mp, nb, NB, Vp, Tp, Cn + int64_t(nb1) * m, rest, w.W1b, w.W2b, w.partb, part_cap,
-                            la->aux, df));
+                            la->aux, df, wy ? wy->oz_bulk : nullptr, wy ? wy->oz_bulk_bytes : 0));
       TNX_CUDA(cudaEventRecord(la->ev_r, la->aux));  // panel p+2's columns updated by H_p
     }
     // panel p joins the compact WY form on the lowest-priority stream, off the critical path

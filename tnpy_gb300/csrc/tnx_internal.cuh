@@ -171,6 +171,12 @@ int gemm_df64(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, c
 // FP64-class GEMM on the tensor cores (Ozaki slicing, gemm_oz.cu); workspace sized by
 // gemm_oz_workspace_bytes(m, n, k)
 size_t gemm_oz_workspace_bytes(int64_t m, int64_t n, int64_t k);
+// Batched (grid z over `batch` operand sets at element strides sA, sB, sC; chains with
+// mask[b] == 0 skipped) and split-K (`nsplit` K ranges, partials summed in order) form
+size_t gemm_oz_ex_workspace_bytes(int64_t m, int64_t n, int64_t k, int batch, int nsplit);
+int gemm_oz_ex(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+               int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C, int64_t ldc, int64_t sC,
+               int batch, int nsplit, const int* mask, void* ws, size_t ws_bytes, cudaStream_t st);
 int gemm_oz(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
             const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws, size_t ws_bytes,
             cudaStream_t st);

@@ -300,6 +300,28 @@ def gemm_oz(a: torch.Tensor, b: torch.Tensor, trans_a=False, trans_b=False):
     return out
 
 
+def gemm_oz_batched(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor | None = None, *, alpha=1.0, beta=0.0,
+                    nsplit: int = 1, mask: torch.Tensor | None = None):
+    """C[i] = alpha A[i] B[i] + beta C[i] for stacked [batch, m, k] / [batch, k, n] FP64 tensors in one
+    tensor-core launch (Ozaki), K split into `nsplit` ranges; entries with mask[i] == 0 are left
+    untouched."""
+    a, b = _f64(a, "a"), _f64(b, "b")
+    if a.ndim != 3 or b.ndim != 3 or a.shape[0] != b.shape[0] or a.shape[2] != b.shape[1]:
+        raise ValueError(f"shapes {tuple(a.shape)} and {tuple(b.shape)} do not form a batched product")
+    bt, m, k = a.shape
+    n = b.shape[2]
+    if c is None:
+        c = torch.zeros((bt, m, n), dtype=torch.float64, device=a.device)
+    if mask is not None:
+        mask = mask.to(device=a.device, dtype=torch.int32).contiguous()
+    wp, wn = Workspace.get(lib.tnx_gemm_oz_batched_workspace_bytes(m, n, k, bt, nsplit), a.device)
+    check("tnx_gemm_oz_batched",
+          lib.tnx_gemm_oz_batched(0, 0, m, n, k, float(alpha), ptr(a), k, m * k, ptr(b), n, k * n, float(beta),
+                                  ptr(c), n, m * n, bt, nsplit, ptr(mask) if mask is not None else None, wp, wn,
+                                  stream_ptr()))
+    return c
+
+
 # ---- chains batched in lockstep ([B, ...] stacked tensors; every call spans all chains) ----
 def _stacked(t: torch.Tensor, name: str, nd: int) -> torch.Tensor:
     t = _f64(t, name)
