@@ -569,8 +569,9 @@ int launch_panel(double* F, int64_t m, int64_t j0, int nb, double* tau, double* 
 // for panels too tall for a cluster's shared memory) and arithmetic (df: the double-FP32 panel
 // of the FP64-class modes). Wider panels give the trailing-update GEMMs a longer K; 16-CTA
 // clusters (where the device schedules them) spread the panel over twice the SMs of the
-// portable 8. TNX_QR_CLUSTER=8 or 16 restricts the cluster size and TNX_QR_PANEL=fp64 keeps
-// FP64 panels in the FP64-class modes (tuning).
+// portable 8. TNX_QR_CLUSTER=8 or 16 restricts the cluster size, TNX_QR_PANEL=fp64 keeps
+// FP64 panels in the FP64-class modes and TNX_QR_NB=32 selects 32-column double-FP32 panels
+// (tuning).
 struct PanelPlan {
   int nb, cl;
   bool df;
@@ -592,8 +593,13 @@ PanelPlan plan_panels(int64_t m, bool df) {
     const char* e = getenv("TNX_QR_PANEL");
     return e && std::string(e) == "fp64";
   }();
+  static const int nb_only = [] {
+    const char* e = getenv("TNX_QR_NB");
+    return e ? atoi(e) : 0;
+  }();
   const bool c8 = only == 0 || only == 8, c16 = only == 0 || only == 16;
   if (df && !fp64_panels) {
+    if (nb_only == 32 && c16 && panel_fits<32, 16, true>(m)) return {32, 16, true};
     if (c16 && panel_fits<64, 16, true>(m)) return {64, 16, true};
     if (c8 && panel_fits<64, 8, true>(m)) return {64, 8, true};
   }
@@ -612,8 +618,9 @@ int factor_panel(const PanelPlan& pp, double* F, int64_t m, int64_t j0, int nb, 
     panel_kernel<<<1, QT, 0, st>>>(F, m, j0, nb, tau, T);
     TNX_LAUNCH_CHECK();
   } else if (pp.df) {
-    rc = pp.cl == 16 ? launch_panel<64, 16, true>(F, m, j0, nb, tau, T, st)
-                     : launch_panel<64, 8, true>(F, m, j0, nb, tau, T, st);
+    rc = pp.nb == 32   ? launch_panel<32, 16, true>(F, m, j0, nb, tau, T, st)
+         : pp.cl == 16 ? launch_panel<64, 16, true>(F, m, j0, nb, tau, T, st)
+                       : launch_panel<64, 8, true>(F, m, j0, nb, tau, T, st);
   } else if (pp.nb == 64) {
     rc = pp.cl == 16 ? launch_panel<64, 16, false>(F, m, j0, nb, tau, T, st)
                      : launch_panel<64, 8, false>(F, m, j0, nb, tau, T, st);

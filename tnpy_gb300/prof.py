@@ -66,6 +66,7 @@ def main(argv=None):
     p.add_argument("mode", choices=["matvec", "env", "qr", "gauge", "davidson", "sweep", "tsdrg", "chains", "svd",
                                     "ed"])
     p.add_argument("--batch", type=int, default=64)
+    p.add_argument("--no-families", action="store_true", help="skip the per-family profiled repetitions")
     p.add_argument("--sites", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--chi", type=int, default=1024)
@@ -92,8 +93,15 @@ def main(argv=None):
         for _ in range(a.warmup):
             sweep()
         t = _time(sweep, a.reps)
-        fam = _families(sweep, 1)
+        fam = {} if a.no_families else _families(sweep, 1)
         print(f"sweep XXZ({a.sites}) chi={chi}: {t:.1f} ms per sweep; one sweep per family: " + _fmt(fam))
+        # one more sweep inside an NVTX range: `ncu --nvtx --nvtx-include "profiled sweep/"` captures
+        # exactly its launches
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("profiled sweep")
+        sweep()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         return
     if a.mode == "tsdrg":
         import tnpy_gb300 as tg
@@ -160,7 +168,7 @@ def main(argv=None):
             K.gauge_move(1, site.clone(), nb.clone(), precision="mixed")
 
         t = _time(fn, a.reps)
-        print(f"gauge move df64 chi={chi}: {t:.3f} ms  " + _fmt(_families(fn, a.reps)))
+        print(f"gauge move df64 chi={chi}: {t:.3f} ms  " + ("" if a.no_families else _fmt(_families(fn, a.reps))))
     else:
         stats = {}
 
