@@ -177,6 +177,12 @@ size_t tnx_eigh_batched_workspace_bytes(int batch, int max_size, int keep);
 int tnx_eigh_batched(double* A, const int64_t* offsets, const int* sizes, int batch,
                      int max_size, int keep, double* evals, double* evecs, void* workspace,
                      size_t workspace_bytes, void* stream);
+/* The same for matrices of at most 64 rows in double-FP32 arithmetic (FP64-class, ~2^-47):
+ * matrix and rotations in shared memory, rotation angles from FP32 leading parts made exactly
+ * orthogonal in double-FP32. tSDRG's dense blocks (np.linalg.eigh at tnpy/tsdrg.py:584) in the
+ * mixed precision mode. No workspace. */
+int tnx_eigh_batched_df64(double* A, const int64_t* offsets, const int* sizes, int batch, int max_size, int keep,
+                          double* evals, double* evecs, void* stream);
 
 /* ---- QR / SVD gauge move -----------------------------------------------------------------
  * Householder QR of a row-major m x n matrix (m >= n): Q (m x n, orthonormal columns),

@@ -431,3 +431,32 @@ def test_gemm_oz_batched_split_and_mask(cuda, nsplit):
             assert np.max(np.abs(out[i] - ref) / bound) < 1e-13, i
         else:
             np.testing.assert_array_equal(out[i], c0[i])
+
+
+@pytest.mark.parametrize("sizes,keep", [([4], 4), ([1, 2, 3], 1), ([16, 31, 64], 3), ([64, 64, 40], 32)])
+def test_eigh_batched_df64(cuda, sizes, keep):
+    """Double-FP32 Jacobi (matrices up to 64 rows) against numpy: eigenvalues to 1e-13 of the
+    spectral radius, eigenvectors to 1e-11 in the residual, including a matrix with a
+    degenerate cluster."""
+    import tnpy_gb300.kernels as K
+
+    rng = np.random.RandomState(7 + sum(sizes))
+    mats = []
+    for i, s in enumerate(sizes):
+        a = rng.standard_normal((s, s))
+        a = a + a.T
+        if i == 0 and s >= 4:  # a degenerate pair: two equal eigenvalues
+            w, v = np.linalg.eigh(a)
+            w[1] = w[0]
+            a = (v * w) @ v.T
+            a = 0.5 * (a + a.T)
+        mats.append(a)
+    ev, vec = K.eigh_batched([_t(m, cuda) for m in mats], keep=keep, precision="df64")
+    ev, vec = ev.cpu().numpy(), vec.cpu().numpy()
+    for b, m in enumerate(mats):
+        w, _ = np.linalg.eigh(m)
+        k = min(keep, m.shape[0])
+        np.testing.assert_allclose(ev[b, :k], w[:k], atol=1e-13 * np.abs(w).max())
+        v = vec[b, : m.shape[0], :k]
+        np.testing.assert_allclose(v.T @ v, np.eye(k), atol=1e-12)
+        np.testing.assert_allclose(m @ v, v * ev[b, :k], atol=1e-11 * np.abs(w).max())

@@ -71,13 +71,16 @@ def _oracle_chain(n, seed, h):
 # Random fields (h > 0) break the SU(2) symmetry of the h = 0 chain: with exact multiplets
 # cut by the truncation the kept subspace is not unique and depends on the eigensolver's basis
 # inside the multiplet, so parity is checked on non-degenerate chains.
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("n,chi,seed", [(16, 8, 10000), (24, 4, 10001)])
-def test_random_coupling_chain_vs_oracle(cuda, n, chi, seed):
-    """Random-coupling Heisenberg chain: same merge order and kept spectrum as the CPU restatement."""
+def test_random_coupling_chain_vs_oracle(cuda, n, chi, seed, precision):
+    """Random-coupling Heisenberg chain: same merge order and kept spectrum as the CPU restatement
+    (chi <= 8: every block has at most 64 states, so the mixed form runs every block on the
+    double-FP32 Jacobi)."""
     import tnpy_gb300 as tg
 
     model = tg.model.RandomCouplingHeisenberg(n, delta=1.0, h=0.5, seed=seed)
-    t = tg.TSDRG(model.mpo, chi=chi)
+    t = tg.TSDRG(model.mpo, chi=chi, precision=precision)
     t.run()
     o = ots.TreeTensorNetworkSDRG(_oracle_chain(n, seed, 0.5), chi).run()
     np.testing.assert_allclose(t.evals, o.evals, atol=1e-10)

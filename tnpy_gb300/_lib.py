@@ -67,6 +67,7 @@ SIGNATURES = {
     "tnx_mpo_apply_site": (_int, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _vp]),
     "tnx_eigh_batched_workspace_bytes": (_sz, [_int, _int, _int]),
     "tnx_eigh_batched": (_int, [_vp, _vp, _vp, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
+    "tnx_eigh_batched_df64": (_int, [_vp, _vp, _vp, _int, _int, _int, _vp, _vp, _vp]),
     "tnx_qr_workspace_bytes": (_sz, [_i64, _i64]),
     "tnx_qr": (_int, [_vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
     "tnx_gauge_move_workspace_bytes": (_sz, [_int, _i64, _i64, _i64, _i64]),

@@ -165,11 +165,12 @@ def davidson1_stats() -> dict:
     return {"phase1": out[0], "anchored": out[1], "anchors": out[2], "restarts": out[3]}
 
 
-def eigh_batched(mats: list[torch.Tensor], keep: int):
+def eigh_batched(mats: list[torch.Tensor], keep: int, precision: str = "fp64"):
     """Lowest `keep` eigenpairs of each symmetric matrix (one CTA per matrix).
 
     Returns (evals [batch, keep], evecs [batch, max_size, keep]); for a matrix smaller than
-    `keep` only its own eigenpairs are written (the rest is NaN / zero)."""
+    `keep` only its own eigenpairs are written (the rest is NaN / zero). precision 'df64':
+    double-FP32 Jacobi in shared memory for matrices up to 64 rows (FP64 above)."""
     if not mats:
         raise ValueError("no matrices")
     dev = mats[0].device
@@ -190,6 +191,11 @@ def eigh_batched(mats: list[torch.Tensor], keep: int):
     sizes_t = torch.tensor(sizes, dtype=torch.int32, device=dev)
     evals = torch.full((batch, keep), float("nan"), dtype=torch.float64, device=dev)
     evecs = torch.zeros((batch, max_size, keep), dtype=torch.float64, device=dev)
+    if precision == "df64" and max_size <= 64:
+        check("tnx_eigh_batched_df64", lib.tnx_eigh_batched_df64(ptr(packed), ptr(offsets), ptr(sizes_t), batch,
+                                                                 max_size, keep, ptr(evals), ptr(evecs),
+                                                                 stream_ptr()))
+        return evals, evecs
     nbytes = lib.tnx_eigh_batched_workspace_bytes(batch, max_size, keep)
     wp, wn = Workspace.get(nbytes, dev)
     check("tnx_eigh_batched", lib.tnx_eigh_batched(ptr(packed), ptr(offsets), ptr(sizes_t), batch, max_size,
