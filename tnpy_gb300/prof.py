@@ -6,7 +6,7 @@
     python -m tnpy_gb300.prof gauge --chi 1024       # one-site gauge move (QR with double-FP32 GEMMs)
     python -m tnpy_gb300.prof davidson --chi 512     # one mixed-precision local eigensolve
     python -m tnpy_gb300.prof sweep --chi 1024 --sites 100   # fDMRG sweeps of XXZ(n, -0.5), per family
-    python -m tnpy_gb300.prof tsdrg --sites 128 --chi 32 --batch 64   # batched tSDRG realisations
+    python -m tnpy_gb300.prof tsdrg --sites 128 --chi 32 --batch 64 [--precision mixed]   # batched tSDRG
     python -m tnpy_gb300.prof chains --sites 64 --chi 64 --batch 64   # lockstep fDMRG chains, one sweep
     python -m tnpy_gb300.prof svd --m 2048 --n 1024   # one-sided Jacobi SVD
     python -m tnpy_gb300.prof ed --sites 12           # dense MPO Hamiltonian + full spectrum
@@ -67,6 +67,7 @@ def main(argv=None):
                                     "ed"])
     p.add_argument("--batch", type=int, default=64)
     p.add_argument("--no-families", action="store_true", help="skip the per-family profiled repetitions")
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="tsdrg mode's precision")
     p.add_argument("--sites", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--chi", type=int, default=1024)
@@ -109,10 +110,11 @@ def main(argv=None):
         mpos = [tg.model.RandomCouplingHeisenberg(a.sites, delta=1.0, h=0.0, seed=r).mpo for r in range(a.batch)]
 
         def run():
-            tg.BatchedTSDRG(mpos, chi=chi).run()
+            tg.BatchedTSDRG(mpos, chi=chi, precision=a.precision).run()
 
         t = _time(run, a.reps)
-        print(f"tsdrg n={a.sites} chi={chi} x{a.batch}: {t:.1f} ms per batch ({a.batch / t * 1e3:.1f} realisations/s)")
+        print(f"tsdrg n={a.sites} chi={chi} x{a.batch} {a.precision}: {t:.1f} ms per batch "
+              f"({a.batch / t * 1e3:.1f} realisations/s)")
         return
     if a.mode == "chains":
         import tnpy_gb300 as tg
