@@ -705,8 +705,8 @@ def run_ours(a):
     # region. The headline roofline is the family with the largest share of the step.
     fams = {0: ("bf16x3_gemm_kernel (tcgen05 split-BF16 GEMM of the one-site matvec)", 3.0,
                 "bf16_tflops_sustained / 3 (three BF16 products per split-BF16 product)", f"tc_gemm_chi{a.chi}"),
-            1: ("gemm_df64_kernel + nar_* (double-FP32 SIMT: the QR's next-panel update, small T products, "
-                "the environment's W contractions)", 36.0,
+            1: ("gemm_df64_kernel + nar_* (double-FP32 / FP64 SIMT GEMMs: the QR's next-panel update and "
+                "small T products, products too small for the tensor-core GEMM)", 36.0,
                 "bf16_tflops_sustained / 36, the FP64-class tensor-core bound the Ozaki GEMM runs against "
                 "(this SIMT kernel does the same FP64-class products on the FP32 pipe)", None),
             3: ("qrdf::panel_df_kernel (double-FP32 16-CTA cluster Householder panel)", 36.0,
