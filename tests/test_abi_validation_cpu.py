@@ -81,3 +81,25 @@ def test_noalloc_matvec_rejects_sizes_that_would_overflow(chi_l, d, chi_r, dl, d
     f.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int64] * 5 + [ctypes.c_void_p]
     st = f(P, P, P, P, P, chi_l, d, chi_r, dl, dr, None)
     assert st == L.TNX_ERR_SHAPE, _err()
+
+
+def test_gemm_oz_batched_rejects_bad_arguments():
+    f = L.lib.tnx_gemm_oz_batched
+    assert f(0, 0, -1, 4, 4, 1.0, P, 4, 16, P, 4, 16, 0.0, P, 4, 16, 2, 1, None, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert f(0, 0, 4, 4, 4, 1.0, P, 4, 16, P, 4, 16, 0.0, P, 4, 16, 0, 1, None, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert f(0, 0, 4, 4, 4, 1.0, P, 4, 16, P, 4, 16, 0.0, P, 4, 16, 2, 0, None, None, 0, None) == L.TNX_ERR_INVALID_ARG
+    assert f(0, 0, 4, 4, 4, 1.0, None, 4, 16, P, 4, 16, 0.0, P, 4, 16, 2, 1, None, None, 0, None) == \
+        L.TNX_ERR_INVALID_ARG
+    # one launch covers batch x split CTAs layers: at most 65535
+    assert f(0, 0, 4, 4, 4, 1.0, P, 4, 16, P, 4, 16, 0.0, P, 4, 16, 40000, 2, None, None, 0, None) == \
+        L.TNX_ERR_INVALID_ARG
+    assert "split" in _err()
+
+
+def test_eigh_batched_df64_rejects_bad_arguments():
+    f = L.lib.tnx_eigh_batched_df64
+    assert f(P, P, P, 2, 65, 4, P, P, None) == L.TNX_ERR_SHAPE      # matrices above 64 rows
+    assert "64" in _err()
+    assert f(P, P, P, 2, 16, 17, P, P, None) == L.TNX_ERR_INVALID_ARG  # keep above max_size
+    assert f(None, P, P, 2, 16, 4, P, P, None) == L.TNX_ERR_INVALID_ARG
+    assert f(P, P, P, 0, 16, 4, P, P, None) == L.TNX_OK             # empty batch: nothing to do
