@@ -179,8 +179,8 @@ int tnx_eigh_batched(double* A, const int64_t* offsets, const int* sizes, int ba
                      size_t workspace_bytes, void* stream);
 /* The same for matrices of at most 64 rows in double-FP32 arithmetic (FP64-class, ~2^-47):
  * matrix and rotations in shared memory, rotation angles from FP32 leading parts made exactly
- * orthogonal in double-FP32. tSDRG's dense blocks (np.linalg.eigh at tnpy/tsdrg.py:584) in the
- * mixed precision mode. No workspace. */
+ * orthogonal in double-FP32. A faster FP64-class form of the dense block spectra of tSDRG
+ * (np.linalg.eigh at tnpy/tsdrg.py:584); no workspace. */
 int tnx_eigh_batched_df64(double* A, const int64_t* offsets, const int* sizes, int batch, int max_size, int keep,
                           double* evals, double* evecs, void* stream);
 

@@ -74,9 +74,8 @@ def _oracle_chain(n, seed, h):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("n,chi,seed", [(16, 8, 10000), (24, 4, 10001)])
 def test_random_coupling_chain_vs_oracle(cuda, n, chi, seed, precision):
-    """Random-coupling Heisenberg chain: same merge order and kept spectrum as the CPU restatement
-    (chi <= 8: every block has at most 64 states, so the mixed form runs every block on the
-    double-FP32 Jacobi)."""
+    """Random-coupling Heisenberg chain: same merge order and kept spectrum as the CPU restatement,
+    in both precision modes (chi <= 8: every block is a dense solve)."""
     import tnpy_gb300 as tg
 
     model = tg.model.RandomCouplingHeisenberg(n, delta=1.0, h=0.5, seed=seed)

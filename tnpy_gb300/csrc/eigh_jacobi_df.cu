@@ -1,6 +1,6 @@
-// Dense symmetric eigensolver for small matrices (n <= 64) in double-FP32 arithmetic: the
-// FP64-class form of the batched Jacobi used for tSDRG's dense block spectra
-// (np.linalg.eigh at tnpy/tsdrg.py:584) in the mixed precision mode.
+// Dense symmetric eigensolver for small matrices (n <= 64) in double-FP32 arithmetic: an
+// FP64-class form of the batched Jacobi behind tSDRG's dense block spectra (np.linalg.eigh at
+// tnpy/tsdrg.py:584), selected by eigh_batched(..., precision="df64").
 //
 // One CTA per matrix, the matrix and the rotation accumulator V held in shared memory as
 // (hi, lo) float pairs, parallel cyclic Jacobi with the round-robin ordering of the FP64

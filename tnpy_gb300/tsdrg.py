@@ -304,19 +304,24 @@ def _select(c: "_Chain", ev: np.ndarray, vec: torch.Tensor):
     return e_k[idx].copy(), (vec[:, torch.from_numpy(sel).to(vec.device)] * sign[None, :]).contiguous()
 
 
+# Dense block eigensolver: the FP64 Jacobi in every precision mode. The double-FP32 Jacobi
+# ('df64', 2.1x faster per 64-state block) changes, on SU(2)-symmetric chains (h = 0), which
+# members of degenerate multiplets are kept; on the n=128, chi=32 bench chains the resulting
+# trees merge more 32 x 32 blocks, whose Kronecker solves cost more than the Jacobi saves
+# (44.6 against 90 realisations/s), so it is not the default.
+_dense_precision = "fp64"
+
+
 def _dense(idx, chains_bonds, out, dev):
-    """Dense Jacobi solve of the listed blocks (block_hamiltonian + eigh, tsdrg.py:569-631): FP64,
-    or double-FP32 for blocks of up to 64 states when every chain runs in the mixed precision;
-    the variants' blocks are solved in full and their kept pairs selected by _select."""
+    """Dense Jacobi solve of the listed blocks (block_hamiltonian + eigh, tsdrg.py:569-631); the
+    variants' blocks are solved in full and their kept pairs selected by _select."""
     pairs = [(chains_bonds[i][0].cache[chains_bonds[i][1]], chains_bonds[i][0].cache[chains_bonds[i][1] + 1])
              for i in idx]
     mats, sizes = block_hamiltonians(pairs, dev)
     full = any(chains_bonds[i][0].mode != "lowest" for i in idx)
     chi = max(chains_bonds[i][0].chi for i in idx)
     keep = max(sizes) if full else min(chi, max(sizes))
-    # mixed chains: blocks up to 64 states on the double-FP32 Jacobi (FP64-class, FP32 pipe)
-    mixed = all(chains_bonds[i][0].precision == "mixed" for i in idx)
-    evals, evecs = K.eigh_batched(mats, keep=keep, precision="df64" if mixed else "fp64")
+    evals, evecs = K.eigh_batched(mats, keep=keep, precision=_dense_precision)
     ev_h = evals.cpu().numpy()
     for j, (i, m) in enumerate(zip(idx, sizes)):
         c = chains_bonds[i][0]
@@ -420,12 +425,11 @@ class TreeTensorNetworkSDRG:
     def __init__(self, mpo: MatrixProductOperator, chi: int, device=None, precision: str = "fp64"):
         """tsdrg.py:500-528; all tensors live on ``device`` (default: current CUDA device).
 
-        ``precision``: 'fp64' (default) solves blocks of up to 64 states by the dense FP64 Jacobi
-        and runs the Kronecker subspace iteration of larger blocks in FP32, finished in FP64,
-        matching the reference's FP64 eigh; 'mixed' solves the small blocks by the double-FP32
-        Jacobi (FP64-class on the FP32 pipe) and stops the Kronecker iteration after its FP32
-        stage (+ FP64 Rayleigh-Ritz), several times faster with kept spectra accurate to ~1e-7
-        relative on large clustered blocks."""
+        ``precision`` for blocks above 64 states (smaller blocks are dense FP64 Jacobi solves):
+        'fp64' (default) runs the Kronecker subspace iteration in FP32 and finishes it in FP64,
+        matching the reference's FP64 eigh; 'mixed' stops after the FP32 iteration (+ FP64
+        Rayleigh-Ritz), several times faster with kept spectra accurate to ~1e-7 relative on
+        large clustered blocks."""
         self._mpo = mpo
         self._chi = int(chi)
         self._dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
