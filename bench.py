@@ -315,7 +315,7 @@ def fp64_sweep(f, direction, tol: float, mixed_s: float):
     return out
 
 
-def config1_line(with_cpu: bool):
+def xxz_n32_line(with_cpu: bool):
     """Plain FP64 fDMRG of XXZ(32, delta=-0.5) (H = sum SxSx + SySy + 0.5 SzSz up to a sublattice
     rotation), chi=32, seeded random MPS, tol 1e-8, at most 10 sweeps: seconds per sweep on the
     GPU, the same run of the CPU restatement timed beside it, their final energies, and the ED
@@ -357,8 +357,8 @@ def config1_line(with_cpu: bool):
     return out
 
 
-def config2_ramp_line(precision: str = "mixed"):
-    """Config 2's chi ramp on XXZ(100, delta=-0.5): chi 256 -> 512 -> 1024 from the seeded random
+def chi_ramp_line(precision: str = "mixed"):
+    """The chi ramp on XXZ(100, delta=-0.5): chi 256 -> 512 -> 1024 from the seeded random
     MPS, two sweeps per stage and then sweeps to |dE| < 1e-8 at chi=1024 (FiniteDMRG.ramp): per
     stage the sweeps, seconds, energy, middle-bond truncation error (weight beyond the previous
     chi) and smallest kept Schmidt weight, and the time to solution of the whole ramp."""
@@ -383,7 +383,7 @@ def config2_ramp_line(precision: str = "mixed"):
     return out
 
 
-def config3_line(with_cpu: bool):
+def random_field_line(with_cpu: bool):
     """Random-field Heisenberg RandomHeisenberg(200, h=3, seed=7), chi=512: the mixed form with
     FP32 environment storage swept to convergence from the seeded random MPS, then the plain
     FP64 form converged from a copy of that state; seconds per sweep of each, |dE|/|E|, the
@@ -507,7 +507,7 @@ def tsdrg_rate(n_real: int, with_cpu: bool, n_single: int = 16):
 
 
 def chains_rate(n_chains: int, with_cpu: bool, n_single: int = 4, precision: str = "mixed"):
-    """Config 5: RandomHeisenberg(64, h=1, seed=100+c) chains at chi=64 swept in lockstep
+    """Many independent chains: RandomHeisenberg(64, h=1, seed=100+c) at chi=64 swept in lockstep
     (BatchedFiniteDMRG: every kernel spans all chains, per-chain Davidson convergence masks) to
     |dE| < 1e-8 per chain (at most 10 sweeps), in the batched mixed form (double-FP32 products
     on the FP32 pipe, FP64 Rayleigh-Ritz); against one chain per launch sequence (FiniteDMRG per
@@ -774,9 +774,9 @@ def run_ours(a):
     if rank == 0 and not a.no_extras:
         line["matvec_forms"] = matvec_forms(f, a.n // 2)
         line["fp64_sweep"] = fp64_sweep(f, dirs[step % 2], a.tol, t_step)
-        line["config1"] = config1_line(with_cpu=(world == 1 and not a.no_cpu))
-        line["config2_ramp"] = config2_ramp_line()
-        line["config3"] = config3_line(with_cpu=(world == 1 and not a.no_cpu))
+        line["xxz_n32_chi32_fp64"] = xxz_n32_line(with_cpu=(world == 1 and not a.no_cpu))
+        line["xxz_n100_chi_ramp"] = chi_ramp_line()
+        line["random_heisenberg_n200_chi512"] = random_field_line(with_cpu=(world == 1 and not a.no_cpu))
         line["tsdrg"] = tsdrg_rate(a.tsdrg_realizations, with_cpu=(world == 1 and not a.no_cpu))
         line["chains"] = chains_rate(a.chains, with_cpu=(world == 1 and not a.no_cpu))
     if rank == 0 and world == 1 and not a.no_cpu:

@@ -65,7 +65,7 @@ def test_fp32_environments_are_stored_fp32(cuda):
         tg.FiniteDMRG(tg.model.XXZ(8, 0.5).mpo, bond_dim=8, env_precision="fp16")
 
 
-def test_config3_n200_chi512_spectrum_mixed_fp32_env_vs_fp64(cuda):
+def test_random_field_n200_chi512_spectrum_mixed_fp32_env_vs_fp64(cuda):
     """n=200, chi=512: mixed form with FP32 environments swept to convergence from the seeded
     random MPS; the FP64 form then converges from a copy of that state. Middle-bond
     entanglement spectra agree within 2e-6 (the FP32 rounding of the stored environments, first

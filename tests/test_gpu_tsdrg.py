@@ -154,7 +154,8 @@ def test_chain_n64_chi32_fp64_vs_oracle(cuda):
 
 @pytest.mark.parametrize("seed", [10000, 10007])
 def test_batched_n128_chi32_kept_spectra_vs_one_at_a_time_fp64(cuda, seed):
-    """Config 4's comparison on the h != 0 variant (h = 0 is SU(2) symmetric and chi = 32 cuts
+    """The batched-vs-one-at-a-time comparison of n = 128, chi = 32 chains on the h != 0 variant
+    (h = 0 is SU(2) symmetric and chi = 32 cuts
     through exact multiplets, where the kept subspace is not unique): n = 128, chi = 32, delta = 1
     random couplings with fields h_i ~ U[-0.5, 0.5). The batched FP64 run (two realisations in one
     lockstep launch sequence) keeps the same spectra as the one-block-at-a-time FP64 numpy eigh

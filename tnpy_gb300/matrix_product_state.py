@@ -135,7 +135,7 @@ class MatrixProductState:
 
     def save(self, filename: str):
         """Reference-shaped tensors in site order to ``.npz`` (matrix_product_state.py:118-142;
-        ``.hdf5`` needs h5py, which this build does not use)."""
+        ``.hdf5`` needs h5py, which the library does not use)."""
         path = Path(filename)
         if path.suffix != ".npz":
             raise ValueError(f"File extension {path.suffix} is not supported.")
