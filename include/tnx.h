@@ -138,6 +138,15 @@ int tnx_davidson1(const double* L, const double* W, const double* R, double* x, 
                   int64_t d, int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter,
                   int max_basis, int precision, double* eval_out, double* resid_out,
                   int* iters_out, void* workspace, size_t workspace_bytes, void* stream);
+/* tnx_davidson1 with flags. TNX_DAV_START_ANCHORED (mixed precision only): x is expected to be
+ * the answer already (the site converged in the previous sweep); the solve starts with the
+ * FP64-class anchor product and skips the first split-BF16 phase, which would hand over after
+ * its first product. The result and its certification are those of tnx_davidson1. */
+#define TNX_DAV_START_ANCHORED 1
+int tnx_davidson1_ex(const double* L, const double* W, const double* R, double* x, int64_t chi_l, int64_t d,
+                     int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter, int max_basis, int precision,
+                     int flags, double* eval_out, double* resid_out, int* iters_out, void* workspace,
+                     size_t workspace_bytes, void* stream);
 /* Generalised problem A x = lambda B x, lowest lambda, for shift-invert DMRG
  * (ShiftInvertDMRG.one_site_solver -> primme.eigsh(A, M=B), tnpy/finite_dmrg.py:345-363): A is
  * the one-site H_eff of (L, W, R), B that of (L2, W2, R2) (environments of the MPO square,

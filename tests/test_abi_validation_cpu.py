@@ -103,3 +103,10 @@ def test_eigh_batched_df64_rejects_bad_arguments():
     assert f(P, P, P, 2, 16, 17, P, P, None) == L.TNX_ERR_INVALID_ARG  # keep above max_size
     assert f(None, P, P, 2, 16, 4, P, P, None) == L.TNX_ERR_INVALID_ARG
     assert f(P, P, P, 0, 16, 4, P, P, None) == L.TNX_OK             # empty batch: nothing to do
+
+
+def test_davidson_ex_rejects_unknown_flags():
+    ev, rn, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    st = L.lib.tnx_davidson1_ex(P, P, P, P, 4, 2, 4, 5, 5, 1e-8, 100, 24, 1, 2, ctypes.byref(ev), ctypes.byref(rn),
+                                ctypes.byref(it), None, 0, None)
+    assert st == L.TNX_ERR_INVALID_ARG and "flags" in _err()

@@ -76,18 +76,25 @@ class _FakeSolverSite:
     """Stands in for the device pieces of one_site_solver: a site tensor, an environment whose
     site_operator returns placeholders, and a scripted davidson1."""
 
-    def __init__(self, results, monkeypatch):
+    def __init__(self, results, monkeypatch, stats=None):
         import tnpy_gb300.kernels as K
 
         self.calls = []
+        self.anchored = []
         it = iter(results)
+        st = iter(stats or [])
 
-        def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64", raise_on_fail=False):
+        def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64", raise_on_fail=False,
+                      start_anchored=False):
             self.calls.append(precision)
+            self.anchored.append(start_anchored)
             return next(it)
 
         monkeypatch.setattr(K, "davidson1", davidson1)
+        monkeypatch.setattr(K, "davidson1_stats",
+                            lambda: next(st, {"phase1": 3, "anchored": 2, "anchors": 1, "restarts": 0}))
         f = FiniteDMRG.__new__(FiniteDMRG)
+        f._settled = {}
         f._exact_solver_dim = 200
         f.max_iter, f.max_basis = 400, 24
         f.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0, "df64_retries": 0}
@@ -127,3 +134,19 @@ def test_unconverged_solve_can_raise(monkeypatch):
     s.f.precision = "fp64"
     with pytest.raises(RuntimeError):
         s.f.one_site_solver(0, 1e-8, raise_on_fail=True)
+
+
+def test_settled_site_starts_at_the_anchor(monkeypatch):
+    """A mixed solve that converged at its first anchor with no split-BF16 expansion marks its
+    site settled; the next solve there starts with the anchor (start_anchored), and a solve that
+    needed more clears the mark."""
+    settled = {"phase1": 1, "anchored": 0, "anchors": 1, "restarts": 0}
+    busy = {"phase1": 6, "anchored": 3, "anchors": 2, "restarts": 0}
+    s = _FakeSolverSite([(-1.0, 1e-9, 1, True), (-1.0, 1e-9, 0, True), (-1.0, 1e-9, 9, True),
+                         (-1.0, 1e-9, 9, True)], monkeypatch,
+                        stats=[settled, dict(settled, phase1=0), busy, busy])
+    s.f.precision = "mixed"
+    for _ in range(4):
+        s.f.one_site_solver(0, 1e-8)
+    assert s.anchored == [False, True, True, False]
+    assert s.f.stats["anchored_starts"] == 2

@@ -60,6 +60,8 @@ SIGNATURES = {
     "tnx_davidson1_workspace_bytes": (_sz, [_i64, _i64, _i64, _i64, _i64, _int, _int]),
     "tnx_davidson1": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _dbl, _int, _int, _int,
                              _pd, _pd, _pi, _vp, _sz, _vp]),
+    "tnx_davidson1_ex": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _dbl, _int, _int, _int, _int,
+                                _pd, _pd, _pi, _vp, _sz, _vp]),
     "tnx_davidson1_stats": (_int, [_pi]),
     "tnx_gdavidson1_workspace_bytes": (_sz, [_i64, _i64, _i64, _i64, _i64, _i64, _i64, _int]),
     "tnx_gdavidson1": (_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _i64, _i64, _dbl,

@@ -387,7 +387,7 @@ thread_local DavStats g_dav_stats;
 int davidson1(const double* L, const double* W, const double* R, double* x_io, int64_t chi_l, int64_t d,
               int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter, int mb, int precision,
               double* eval_out, double* resid_out, int* iters_out, void* ws, size_t ws_bytes,
-              cudaStream_t st) {
+              cudaStream_t st, int flags = 0) {
   DavWs w;
   const size_t need = dav_layout(chi_l, d, chi_r, dl, dr, mb, precision, ws, ws_bytes, &w);
   if (ws_bytes < need || !ws) {
@@ -400,6 +400,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   if (mb > n) mb = int(n);
   if (mb < 2) mb = 2;
   const bool mixed = precision == TNX_BF16X3 && w.mv != nullptr;
+  // mixed form, start vector expected at the answer (the site converged in the previous sweep):
+  // certify it with the FP64-class anchor at once instead of a first split-BF16 phase that
+  // would only hand over after its first product
+  const bool start_anchored = mixed && (flags & TNX_DAV_START_ANCHORED);
   int* dflag = nullptr;
   if (mixed) {
     TNX_TRY(mixed_prepare(L, R, chi_l, d, chi_r, dl, dr, w.mv, st));
@@ -617,7 +621,8 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // max(tol, 2e-7) |theta|: the energy error is quadratic in the residual,
   // ~ (2e-7 |theta|)^2 / gap, i.e. below 1e-12 |E| for local gaps above 1e-2.
   const double mixed_handover = 3e-6, mixed_near_floor = 1e-4, mixed_rtol = tol > 2e-7 ? tol : 2e-7;
-  for (;;) {
+  if (start_anchored) TNX_CUDA(cudaMemcpyAsync(w.x, x_io, n * 8, cudaMemcpyDeviceToDevice, st));
+  for (; !start_anchored;) {
     bool fell_in = false;
     TNX_TRY(f32 ? expand(v32, false, &fell_in) : expand(v64, false, &fell_in));
     if (fell_in) {
@@ -685,7 +690,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     const double eps_h = 3e-5;  // bound on the split-BF16 matvec error relative to |H|
     converged = false;
     for (int anchor = 0;; ++anchor) {
-      if (anchor == 0 && f32) {
+      if (anchor == 0 && f32 && !start_anchored) {
         convert_kernel<float, double><<<sblocks, DT, 0, st>>>(v32.x, w.V, n);
         TNX_LAUNCH_CHECK();
       } else {
@@ -987,6 +992,23 @@ int tnx_davidson1(const double* L, const double* W, const double* R, double* x, 
   TNX_CHECK_SHAPE(dl * d <= 64 && dr * d <= 64, "MPO bond too large");
   return davidson1(L, W, R, x, chi_l, d, chi_r, dl, dr, tol, max_iter, max_basis, precision, eval_out,
                    resid_out, iters_out, workspace, workspace_bytes, as_stream(stream));
+}
+
+int tnx_davidson1_ex(const double* L, const double* W, const double* R, double* x, int64_t chi_l, int64_t d,
+                     int64_t chi_r, int64_t dl, int64_t dr, double tol, int max_iter, int max_basis, int precision,
+                     int flags, double* eval_out, double* resid_out, int* iters_out, void* workspace,
+                     size_t workspace_bytes, void* stream) {
+  TNX_CHECK_ARG(L && W && R && x, "null pointer");
+  TNX_CHECK_ARG(chi_l > 0 && d > 0 && chi_r > 0 && dl > 0 && dr > 0, "non-positive dimension");
+  TNX_CHECK_ARG(max_basis >= 2 && max_basis <= MAXB, "max_basis must be in [2, %d] (got %d)", MAXB,
+                max_basis);
+  TNX_CHECK_ARG(max_iter >= 1, "max_iter must be >= 1");
+  TNX_CHECK_ARG(tol >= 0.0, "tol must be >= 0");
+  TNX_CHECK_ARG(precision >= TNX_FP64 && precision <= TNX_DF64, "unknown precision %d", precision);
+  TNX_CHECK_ARG((flags & ~TNX_DAV_START_ANCHORED) == 0, "unknown flags 0x%x", flags);
+  TNX_CHECK_SHAPE(dl * d <= 64 && dr * d <= 64, "MPO bond too large");
+  return davidson1(L, W, R, x, chi_l, d, chi_r, dl, dr, tol, max_iter, max_basis, precision, eval_out,
+                   resid_out, iters_out, workspace, workspace_bytes, as_stream(stream), flags);
 }
 
 }  // extern "C"

@@ -88,6 +88,8 @@ class FiniteDMRG:
         self.sweep_seconds: list[float] = []
         self.stats = {"matvecs": 0, "dense_solves": 0, "iterative_solves": 0, "unconverged": 0,
                       "df64_retries": 0}
+        # sites whose last mixed solve converged at its first anchor, with no split-BF16 expansion
+        self._settled: dict[int, bool] = {}
 
     # ---- properties (finite_dmrg.py:78-95) ----------------------------------------------
     @property
@@ -143,8 +145,15 @@ class FiniteDMRG:
         max_iter = kwargs.get("max_iter", self.max_iter)
         max_basis = kwargs.get("max_basis", self.max_basis)
         precision = kwargs.get("precision", self.precision)
+        # a site whose last solve needed nothing beyond the anchor's certification starts there
+        mixed = K.precision_code(precision) == K.precision_code("mixed")
+        start_anchored = mixed and self._settled.get(site, False)
         e, rn, its, ok = K.davidson1(L, W, R, psi, tol=tol, max_iter=max_iter, max_basis=max_basis,
-                                     precision=precision)
+                                     precision=precision, start_anchored=start_anchored)
+        if mixed:
+            st = K.davidson1_stats()
+            self._settled[site] = bool(ok and st["anchored"] == 0 and st["anchors"] == 1 and st["phase1"] <= 1)
+            self.stats["anchored_starts"] = self.stats.get("anchored_starts", 0) + int(start_anchored)
         self.stats["matvecs"] += its
         if not ok and K.precision_code(precision) == K.precision_code("mixed"):
             self.stats["df64_retries"] += 1
@@ -171,6 +180,7 @@ class FiniteDMRG:
         self.mps.enlarge_bond_dim(new_bond_dim, seed=seed)
         self._bond_dim = int(new_bond_dim)
         self._env.rebuild()
+        self._settled.clear()
 
     def ramp(self, bond_dims, sweeps_per_stage: int = 2, tol: float = 1e-8, max_sweep: int = 20,
              bond: int | None = None, **kwargs) -> list[dict]:

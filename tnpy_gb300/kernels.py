@@ -101,9 +101,12 @@ def env_update(direction: int, E, A, W, out=None, precision="fp64"):
     return out
 
 
-def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64", raise_on_fail=False):
+def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64", raise_on_fail=False,
+              start_anchored=False):
     """Lowest eigenpair of H_eff starting from x (overwritten with the unit eigenvector).
 
+    ``start_anchored`` (mixed precision): x is expected to be the answer already; the solve
+    starts with the FP64-class anchor product instead of a split-BF16 phase.
     Returns (eigenvalue, residual norm, matvec count, converged)."""
     L, W, R = _f64(L, "L"), _f64(W, "W"), _f64(R, "R")
     if x.dtype != torch.float64 or not x.is_cuda or not x.is_contiguous():
@@ -115,9 +118,9 @@ def davidson1(L, W, R, x, tol=1e-8, max_iter=200, max_basis=24, precision="fp64"
     ev = ctypes.c_double(0.0)
     rn = ctypes.c_double(0.0)
     it = ctypes.c_int(0)
-    st = lib.tnx_davidson1(ptr(L), ptr(W), ptr(R), ptr(x), chi_l, d, chi_r, dl, dr, float(tol), int(max_iter),
-                           int(max_basis), p, ctypes.byref(ev), ctypes.byref(rn), ctypes.byref(it), wp, wn,
-                           stream_ptr())
+    st = lib.tnx_davidson1_ex(ptr(L), ptr(W), ptr(R), ptr(x), chi_l, d, chi_r, dl, dr, float(tol), int(max_iter),
+                              int(max_basis), p, 1 if start_anchored else 0, ctypes.byref(ev), ctypes.byref(rn),
+                              ctypes.byref(it), wp, wn, stream_ptr())
     converged = st == _lib.TNX_OK
     if st != _lib.TNX_OK and (st != _lib.TNX_ERR_NOT_CONVERGED or raise_on_fail):
         check("tnx_davidson1", st)
