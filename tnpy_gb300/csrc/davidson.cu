@@ -405,10 +405,6 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   // would only hand over after its first product
   const bool start_anchored = mixed && (flags & TNX_DAV_START_ANCHORED);
   int* dflag = nullptr;
-  if (mixed) {
-    TNX_TRY(mixed_prepare(L, R, chi_l, d, chi_r, dl, dr, w.mv, st));
-    mixed_flag(w.mv, chi_l, d, chi_r, dl, dr, &dflag);
-  }
   // Vector storage of the current phase. The mixed form's first phase (split-BF16 products,
   // converged only to ~3e-6) keeps its basis, Ritz vector and residual in FP32 views of the
   // same buffers: half the bytes, and FP32 instead of FP64-pipe arithmetic in every vector
@@ -439,11 +435,36 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
   double* rn2 = w.scal + MAXB + 2;  // ||r||^2
   double host[4];
 
-  if (int e = tnx_diag1(L, W, R, w.diag, chi_l, d, chi_r, dl, dr, st); e != TNX_OK) return e;
+  // Operands of the expansions: the split-BF16 layout of L and R (mixed form), diag(H) for the
+  // preconditioner and max |diag H| for the operator scale. A settled site that the first anchor
+  // certifies needs none of them, so they are prepared on first use.
+  bool prepared = false;
+  double hdiag = 0.0;
+  auto prepare = [&]() -> int {
+    if (prepared) return TNX_OK;
+    prepared = true;
+    if (mixed) {
+      TNX_TRY(mixed_prepare(L, R, chi_l, d, chi_r, dl, dr, w.mv, st));
+      mixed_flag(w.mv, chi_l, d, chi_r, dl, dr, &dflag);
+    }
+    if (int e = tnx_diag1(L, W, R, w.diag, chi_l, d, chi_r, dl, dr, st); e != TNX_OK) return e;
+    if (f32) {
+      convert_kernel<double, float><<<sblocks, DT, 0, st>>>(w.diag, w.diag32, n);
+      TNX_LAUNCH_CHECK();
+    }
+    // max |diag H|: with 2 |theta| it estimates |H| for the floors and bounds below (the
+    // diagonal alone is a lower bound of the spectral radius and catches operators whose lowest
+    // eigenvalue is small against their width)
+    absmax_kernel<<<nch, DT, 0, st>>>(w.diag, n, w.part, nch);
+    TNX_LAUNCH_CHECK();
+    max_reduce_kernel<<<1, 32, 0, st>>>(w.part, nch, w.scal + MAXB + 3);
+    TNX_LAUNCH_CHECK();
+    TNX_CUDA(cudaMemcpyAsync(&hdiag, w.scal + MAXB + 3, 8, cudaMemcpyDeviceToHost, st));
+    TNX_CUDA(cudaStreamSynchronize(st));
+    return TNX_OK;
+  };
   if (f32) {
     convert_kernel<double, float><<<sblocks, DT, 0, st>>>(x_io, v32.t, n);
-    TNX_LAUNCH_CHECK();
-    convert_kernel<double, float><<<sblocks, DT, 0, st>>>(w.diag, w.diag32, n);
     TNX_LAUNCH_CHECK();
   } else {
     TNX_CUDA(cudaMemcpyAsync(w.t, x_io, n * 8, cudaMemcpyDeviceToDevice, st));
@@ -589,16 +610,7 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
     return TNX_OK;
   };
 
-  // max |diag H|: with 2 |theta| it estimates |H| for the floors and bounds below (the diagonal
-  // alone is a lower bound of the spectral radius and catches operators whose lowest eigenvalue
-  // is small against their width)
-  absmax_kernel<<<nch, DT, 0, st>>>(w.diag, n, w.part, nch);
-  TNX_LAUNCH_CHECK();
-  max_reduce_kernel<<<1, 32, 0, st>>>(w.part, nch, w.scal + MAXB + 3);
-  TNX_LAUNCH_CHECK();
-  double hdiag = 0.0;
-  TNX_CUDA(cudaMemcpyAsync(&hdiag, w.scal + MAXB + 3, 8, cudaMemcpyDeviceToHost, st));
-  TNX_CUDA(cudaStreamSynchronize(st));
+  if (!start_anchored) TNX_TRY(prepare());
   auto hscale = [&]() { return fmax(fmax(2.0 * fabs(theta), hdiag), 1.0); };
 
   bool converged = false;
@@ -718,6 +730,10 @@ int davidson1(const double* L, const double* W, const double* R, double* x_io, i
         break;
       }
       if (anchor >= max_anchor || iters >= max_iter) break;
+      if (!prepared) {  // anchored start that needs expansions: operands, then the correction again
+        TNX_TRY(prepare());
+        TNX_TRY(rayleigh_ritz(v64));
+      }
       best = rnorm;
       best_it = iters;
       // The bound decides whether a converged residual is accepted and, within 100x of the
