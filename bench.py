@@ -711,10 +711,13 @@ def run_ours(a):
                 "(this SIMT kernel does the same FP64-class products on the FP32 pipe)", None),
             3: ("qrdf::panel_df_kernel (double-FP32 16-CTA cluster Householder panel)", 36.0,
                 "bf16_tflops_sustained / 36 (FP64-class tensor-core bound)", None),
-            6: ("oz_gemm_kernel (tcgen05 FP64-class GEMM, 36 exact BF16 slice products)", 36.0,
-                "bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class product)", f"oz_gemm_chi{a.chi}")}
+            6: ("oz_gemm_kernel (tcgen05 FP64-class GEMM, 36 exact BF16 slice products: environment updates, "
+                "anchor matvecs, the gauge move's X, Q and R A)", 36.0,
+                "bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class product)", f"oz_gemm_chi{a.chi}"),
+            7: ("oz_gemm_kernel[narrow] (the same kernel on the QR's K = 64 and split-K trailing / WY products)",
+                36.0, "bf16_tflops_sustained / 36 (36 BF16 slice products per FP64-class product)", None)}
     prof = {6: (n_o.value, ms_o.value, fl_o.value, dev_ms, a.steps)}
-    for fam in (0, 1, 3):
+    for fam in (0, 1, 3, 7):
         lib.tnx_profile_begin(fam)
         sw0, sw1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         sw0.record()
@@ -759,7 +762,8 @@ def run_ours(a):
             "vs_baseline": None, "dtype": "f64 (split-bf16 tensor-core matvec, FP64-class environments / gauge "
             "moves, FP64 eigensolver)" if a.precision == "mixed" else "f64",
             "data": "synthetic (seeded random initial MPS, XXZ MPO)", "config": workload(a),
-            "roofline": rooflines[top], "roofline_ozaki": rooflines[6], "roofline_matvec": rooflines[0],
+            "roofline": rooflines[top], "roofline_ozaki": rooflines[6], "roofline_ozaki_narrow": rooflines[7],
+            "roofline_matvec": rooflines[0],
             "step_shares": shares, "clocks": clk, "gpu_launches": int(launches),
             "e2e": {"value": world / e2e_t, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d + 8},

@@ -57,8 +57,9 @@ long long tnx_launch_count(void);
 /* Time every launch of one kernel family with CUDA events on its stream until
  * tnx_profile_end, which synchronises and returns the launch count, the summed device
  * time and the summed algorithmic flops / bytes of those launches.
- * Families: 0 tcgen05 split-BF16 GEMM, 1 FP64 GEMM, 2 Davidson vector kernels,
- * 3 QR panel, 4 dense eigensolver, 5 other. */
+ * Families: 0 tcgen05 split-BF16 GEMM, 1 FP64 / double-FP32 SIMT GEMM, 2 Davidson vector
+ * kernels, 3 QR panel, 4 dense eigensolver, 5 other, 6 Ozaki FP64-class GEMM (large products),
+ * 7 Ozaki FP64-class GEMM (narrow products: a side of 128 or less, split K, batches). */
 int tnx_profile_begin(int family);
 int tnx_profile_end(int* launches, double* total_ms, double* flops, double* bytes);
 

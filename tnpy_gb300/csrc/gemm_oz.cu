@@ -22,7 +22,8 @@
 // Kernel: one 128 x 64 output tile per CTA, 6 warps: warp 0 TMA producer (all 2 S slice tiles of
 // a 32-deep K block per stage, 2 stages of 96 KB, 64-byte swizzle), warp 1 TMEM allocation (512
 // columns: eight 64-column group accumulators) and single-thread tcgen05.mma issue of the 36
-// slice products per K block, warps 2-5 epilogue. All
+// slice products per K block as 12 MMAs per 16-deep step (slice q of A against the B slices
+// 0..7-q at once, N up to 256), warps 2-5 epilogue. All
 // mbarrier waits are bounded (~2 s); on expiry the kernel raises the error flag and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -135,7 +136,13 @@ __global__ void oz_slice_kernel(const double* __restrict__ src, int64_t rows, in
 // ---------------------------------------------------------------- GEMM kernel
 // Stage layout (one K block of 32): A slices 0..S-1 (128 x 32 bf16, 8 KB each), then B slices
 // 0..S-1 (64 x 32 bf16, 4 KB each), 64-byte swizzle; every slice tile is loaded once per K
-// block and feeds all S(S+1)/2 slice products that use it.
+// block and feeds all S(S+1)/2 slice products that use it. The B slice tiles lie back to back
+// with the same 8-row swizzle groups, so B slices t0..t0+w-1 read as one (64 w) x 32 operand; the
+// group accumulators lie back to back in TMEM (group g at column 64 g), so the products of A
+// slice q with B slices t0..t0+w-1 land in groups q+t0..q+t0+w-1 by one MMA of N = 64 w. Per
+// 16-deep step: A slice q against B slices 0..7-q in MMAs of N <= 256 (2, 2, 2, 2, 1, 1, 1, 1 for
+// q = 0..7), 12 MMAs instead of 36, each A slice read from shared memory once or twice instead of
+// 8 - q times.
 // Batch and split-K: blockIdx.z = bz * nsplit + sz. Chain bz reads its slice planes at plane rows
 // (bz * S + q) * Mp (A) / (bz * S + q) * Np (B) and its exponents at ea + bz Mp / eb + bz Np;
 // split sz covers K blocks [sz kbs, (sz + 1) kbs). With nsplit == 1 the CTA writes
@@ -214,7 +221,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = instr_desc_bf16(OZ_BM, OZ_BN);
       bool ok = true;
       for (int c = 0; c < nchunks && ok; ++c) {
         // the epilogue must have read the previous chunk's accumulators
@@ -238,14 +244,19 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint32_t sa = base + st * STAGE_BYTES, sb = sa + OZ_S * A_TILE;
           const bool chunk_start = kb == c * kb_per_chunk;
-          for (int g = 0; g < OZ_S; ++g) {
-            const uint32_t dst = tmem + uint32_t(g * OZ_BN);
-            for (int q = 0; q <= g; ++q) {  // slice pair (q, g - q)
 #pragma unroll
-              for (int kk = 0; kk < OZ_BK / 16; ++kk) {
-                const uint64_t ad = smem_desc_sw64(sa + q * A_TILE + kk * 32);
-                const uint64_t bd = smem_desc_sw64(sb + (g - q) * B_TILE + kk * 32);
-                mma_bf16(dst, ad, bd, idesc, (chunk_start && q == 0 && kk == 0) ? 0u : 1u);
+          for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+#pragma unroll
+            for (int q = 0; q < OZ_S; ++q) {
+              const uint64_t ad = smem_desc_sw64(sa + q * A_TILE + kk * 32);
+#pragma unroll
+              for (int t0 = 0; t0 < OZ_S - q; t0 += 4) {
+                // slice pairs (q, t0) .. (q, t0 + w - 1) into groups q + t0 .. q + t0 + w - 1; the two
+                // MMAs of (q = 0, kk = 0) cover all eight groups and start a chunk's sums
+                const int w = OZ_S - q - t0 < 4 ? OZ_S - q - t0 : 4;
+                const uint64_t bd = smem_desc_sw64(sb + t0 * B_TILE + kk * 32);
+                mma_bf16(tmem + uint32_t((q + t0) * OZ_BN), ad, bd, instr_desc_bf16(OZ_BM, OZ_BN * w),
+                         (chunk_start && kk == 0 && q == 0) ? 0u : 1u);
               }
             }
           }
@@ -431,7 +442,10 @@ int gemm_oz_ex(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, 
   const int kbs = (kb_all + nsplit - 1) / nsplit;
   nsplit = (kb_all + kbs - 1) / kbs;  // no empty splits
   dim3 grid(unsigned(L.Np / OZ_BN), unsigned(L.Mp / OZ_BM), unsigned(batch * nsplit));
-  profile_mark(KF_OZ_GEMM, st, true);
+  // profiler family: the large products (environment updates, anchor matvecs, the gauge move's
+  // X, Q and R A) apart from the narrow ones (a side of 128 or less, split K, batches)
+  const int fam = (nsplit > 1 || batch > 1 || m <= 128 || n <= 128 || k <= 128) ? KF_OZ_NARROW : KF_OZ_GEMM;
+  profile_mark(fam, st, true);
   oz_gemm_kernel<<<grid, OZ_THREADS, smem, st>>>(ma, mb, int(m), int(n), int(L.Kp), int(L.Mp), int(L.Np), L.ea, L.eb,
                                                  alpha, beta, C, ldc, L.flag, batch, nsplit, kbs, sC, L.part, mask);
   TNX_LAUNCH_CHECK();
@@ -442,9 +456,8 @@ int gemm_oz_ex(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, 
                                                                       beta, C, ldc, sC, mask);
     TNX_LAUNCH_CHECK();
   }
-  profile_mark(KF_OZ_GEMM, st, false);
-  profile_work(KF_OZ_GEMM, 2.0 * double(m) * n * k * batch,
-               8.0 * batch * (double(m) * k + double(k) * n + double(m) * n));
+  profile_mark(fam, st, false);
+  profile_work(fam, 2.0 * double(m) * n * k * batch, 8.0 * batch * (double(m) * k + double(k) * n + double(m) * n));
   return TNX_OK;
 }
 

@@ -51,7 +51,7 @@ void count_launch();
 
 // Optional CUDA-event timing of one kernel family (enabled by tnx_profile_begin).
 enum KernelFamily { KF_TC_GEMM = 0, KF_F64_GEMM = 1, KF_VECTOR = 2, KF_QR_PANEL = 3, KF_EIGH = 4, KF_OTHER = 5,
-                    KF_OZ_GEMM = 6, KF_COUNT = 7 };
+                    KF_OZ_GEMM = 6, KF_OZ_NARROW = 7, KF_COUNT = 8 };
 bool profiling(int family);
 void profile_mark(int family, cudaStream_t st, bool start);
 // algorithmic work (flops, bytes) of the launch just marked, summed while profiling

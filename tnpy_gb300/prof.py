@@ -25,7 +25,8 @@ import torch
 from . import kernels as K
 from ._lib import lib
 
-FAMILIES = ["tcgen05 GEMM", "FP64-class GEMM", "vector", "QR panel", "eigh", "other", "Ozaki GEMM"]
+FAMILIES = ["tcgen05 GEMM", "FP64-class GEMM", "vector", "QR panel", "eigh", "other", "Ozaki GEMM",
+            "Ozaki GEMM (narrow)"]
 
 
 def _families(fn, reps):
