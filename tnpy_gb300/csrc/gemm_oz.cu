@@ -19,11 +19,12 @@
 // double-FP32 summation (~2^-46 of the running sum): FP64-class where rows and columns do not
 // span many decades; at the tensor cores' rate divided by 36.
 //
-// Kernel: one 128 x 64 output tile per CTA, 6 warps: warp 0 TMA producer (all 2 S slice tiles of
+// Kernel: one 128 x 64 output tile per CTA, 10 warps: warp 0 TMA producer (all 2 S slice tiles of
 // a 32-deep K block per stage, 2 stages of 96 KB, 64-byte swizzle), warp 1 TMEM allocation (512
 // columns: eight 64-column group accumulators) and single-thread tcgen05.mma issue of the 36
 // slice products per K block as 12 MMAs per 16-deep step (slice q of A against the B slices
-// 0..7-q at once, N up to 256), warps 2-5 epilogue. All
+// 0..7-q at once, N up to 256), warps 2-9 epilogue (two per TMEM lane quarter, 32 columns
+// each). All
 // mbarrier waits are bounded (~2 s); on expiry the kernel raises the error flag and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -44,7 +45,8 @@ constexpr int OZ_S = 8;                         // slices per operand
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;  // BK = 32 bf16 = one 64-byte swizzle row
 constexpr int OZ_KC = 480;                      // K values per exact accumulation chunk
 constexpr int OZ_STAGES = 2;                    // a stage holds all 2 S slice tiles of one K block
-constexpr int OZ_THREADS = 192;
+constexpr int OZ_EPI_WARPS = 8;                 // two per TMEM lane quarter, 32 columns each
+constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
 constexpr uint32_t OZ_TMEM_COLS = 512;
 
 // ---------------------------------------------------------------- operand slicing
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       mbar_init(smem_u32(&empty_bar[st]), 1);
     }
     mbar_init(smem_u32(&chunk_full), 1);
-    mbar_init(smem_u32(&chunk_empty), 4);
+    mbar_init(smem_u32(&chunk_empty), OZ_EPI_WARPS);
     abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -266,12 +268,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..5): row = lane of quad
+    // ------------------------------------------------ epilogue (warps 2..9): row = lane of the
+    // warp's TMEM lane quarter (warp mod 4), columns cb..cb+31 of every group (two warps a quarter)
     const int quad = warp & 3;
+    const int cb = (warp - 2) / 4 * 32;
     const int row = m0 + quad * 32 + lane;
-    float hi[OZ_BN], lo[OZ_BN];
+    float hi[32], lo[32];
 #pragma unroll
-    for (int j = 0; j < OZ_BN; ++j) hi[j] = lo[j] = 0.f;
+    for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0.f;
     bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
       if (!mbar_wait(smem_u32(&chunk_full), c & 1)) {
@@ -283,18 +287,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll 1
       for (int g = 0; g < OZ_S; ++g) {
         const float scale = __uint_as_float(uint32_t(127 - 7 * (g + 2)) << 23);  // 2^-7(g+2)
+        uint32_t r[32];
+        tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + uint32_t(g * OZ_BN + cb), r);
 #pragma unroll
-        for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
-          uint32_t r[32];
-          tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + uint32_t(g * OZ_BN + c0), r);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float v = __uint_as_float(r[j]) * scale;  // exact: power-of-two scaling
-            float sum, err;
-            two_sum_f(hi[c0 + j], v, sum, err);
-            hi[c0 + j] = sum;
-            lo[c0 + j] += err;
-          }
+        for (int j = 0; j < 32; ++j) {
+          const float v = __uint_as_float(r[j]) * scale;  // exact: power-of-two scaling
+          float sum, err;
+          two_sum_f(hi[j], v, sum, err);
+          hi[j] = sum;
+          lo[j] += err;
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
@@ -305,24 +306,26 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int er = row_scale_exp(ea[row]);
       const bool row_nonfinite = ea[row] == 2047;  // the row holds Inf / NaN: its slices are not the value
       if (nsplit == 1) {
-        double* o = C + int64_t(bz) * sC + int64_t(row) * ldc + n0;
+        double* o = C + int64_t(bz) * sC + int64_t(row) * ldc + n0 + cb;
+        const int* ebc = eb + n0 + cb;
 #pragma unroll
-        for (int j = 0; j < OZ_BN; ++j) {
-          if (n0 + j < N) {
-            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
-            if (row_nonfinite || eb[n0 + j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
+        for (int j = 0; j < 32; ++j) {
+          if (n0 + cb + j < N) {
+            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(ebc[j]));
+            if (row_nonfinite || ebc[j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
             v *= alpha;
             if (beta != 0.0) v = fma(beta, o[j], v);
             o[j] = v;
           }
         }
       } else {
-        double* o = part + (int64_t(sz) * batch + bz) * M * N + int64_t(row) * N + n0;
+        double* o = part + (int64_t(sz) * batch + bz) * M * N + int64_t(row) * N + n0 + cb;
+        const int* ebc = eb + n0 + cb;
 #pragma unroll
-        for (int j = 0; j < OZ_BN; ++j) {
-          if (n0 + j < N) {
-            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(eb[n0 + j]));
-            if (row_nonfinite || eb[n0 + j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
+        for (int j = 0; j < 32; ++j) {
+          if (n0 + cb + j < N) {
+            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(ebc[j]));
+            if (row_nonfinite || ebc[j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
             o[j] = v;
           }
         }
