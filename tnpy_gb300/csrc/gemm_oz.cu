@@ -84,6 +84,13 @@ __global__ void oz_rowmax_kernel(const double* __restrict__ src, int64_t rows, i
 
 __device__ __forceinline__ int row_scale_exp(int bmax) { return bmax > 0 ? bmax - 1021 : 0; }
 
+// x 2^e: one multiplication by the power of two where that is a normal double (exact, or rounded
+// once where the result is subnormal, as ldexp rounds it), ldexp outside that range
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+  if (e >= -1022 && e <= 1023) return x * __longlong_as_double(static_cast<long long>(e + 1023) << 52);
+  return ldexp(x, e);
+}
+
 // bf16 bit pattern of an integer 0 <= q <= 255 (exact)
 __device__ __forceinline__ uint16_t bf16_of_small_int(unsigned q, unsigned sign) {
   if (q == 0u) return 0;
@@ -160,7 +167,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[OZ_STAGES], empty_bar[OZ_STAGES], chunk_full, chunk_empty;
   __shared__ uint32_t tmem_base_sh;
-  __shared__ int abort_sh;
+  __shared__ int abort_sh, epi_fail_sh;
   const int bz = int(blockIdx.z) / nsplit, sz = int(blockIdx.z) % nsplit;
   if (mask && !mask[bz]) return;  // uniform over the CTA, before any barrier or TMEM allocation
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -183,6 +190,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     mbar_init(smem_u32(&chunk_full), 1);
     mbar_init(smem_u32(&chunk_empty), OZ_EPI_WARPS);
     abort_sh = 0;
+    epi_fail_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -268,11 +276,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..9): row = lane of the
-    // warp's TMEM lane quarter (warp mod 4), columns cb..cb+31 of every group (two warps a quarter)
+    // ------------------------------------------------ epilogue (warps 2..9): tile row = lane of
+    // the warp's TMEM lane quarter (warp mod 4), columns cb..cb+31 of every group (two warps a
+    // quarter)
     const int quad = warp & 3;
     const int cb = (warp - 2) / 4 * 32;
-    const int row = m0 + quad * 32 + lane;
     float hi[32], lo[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0.f;
@@ -285,49 +293,60 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
-      for (int g = 0; g < OZ_S; ++g) {
-        const float scale = __uint_as_float(uint32_t(127 - 7 * (g + 2)) << 23);  // 2^-7(g+2)
-        uint32_t r[32];
-        tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + uint32_t(g * OZ_BN + cb), r);
+      for (int g = 0; g < OZ_S; g += 2) {  // two groups' loads in flight per wait
+        uint32_t r[2][32];
+        tmem_ld32_async(tmem + (uint32_t(quad * 32) << 16) + uint32_t(g * OZ_BN + cb), r[0]);
+        tmem_ld32_async(tmem + (uint32_t(quad * 32) << 16) + uint32_t((g + 1) * OZ_BN + cb), r[1]);
+        tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const float v = __uint_as_float(r[j]) * scale;  // exact: power-of-two scaling
-          float sum, err;
-          two_sum_f(hi[j], v, sum, err);
-          hi[j] = sum;
-          lo[j] += err;
+        for (int h = 0; h < 2; ++h) {
+          const float scale = __uint_as_float(uint32_t(127 - 7 * (g + h + 2)) << 23);  // 2^-7(g+h+2)
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float v = __uint_as_float(r[h][j]) * scale;  // exact: power-of-two scaling
+            float sum, err;
+            two_sum_f(hi[j], v, sum, err);
+            hi[j] = sum;
+            lo[j] += err;
+          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&chunk_empty)) : "memory");
     }
-    if (ok && row < M) {
-      const int er = row_scale_exp(ea[row]);
-      const bool row_nonfinite = ea[row] == 2047;  // the row holds Inf / NaN: its slices are not the value
-      if (nsplit == 1) {
-        double* o = C + int64_t(bz) * sC + int64_t(row) * ldc + n0 + cb;
-        const int* ebc = eb + n0 + cb;
+    // the finished tile goes through shared memory (the stage buffers are free once the last
+    // chunk's MMAs are done), so that the global stores are whole row segments: a thread owns one
+    // row of 32 columns in TMEM, and storing from there would write 32 rows per warp instruction
+    if (!ok) epi_fail_sh = 1;
+    double* Cs = reinterpret_cast<double*>(smem_raw + (base - smem_u32(smem_raw)));  // [BM][BN + 1]
+    if (ok) {
+      const int lr = quad * 32 + lane;
+      const int er = row_scale_exp(ea[m0 + lr]);  // ea and eb are padded to Mp and Np entries
+      const bool row_nonfinite = ea[m0 + lr] == 2047;  // the row holds Inf / NaN: its slices are not the value
+      const int* ebc = eb + n0 + cb;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          if (n0 + cb + j < N) {
-            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(ebc[j]));
-            if (row_nonfinite || ebc[j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
+      for (int j = 0; j < 32; ++j) {
+        double v = scale_pow2(join_df(hi[j], lo[j]), er + row_scale_exp(ebc[j]));
+        if (row_nonfinite || ebc[j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
+        Cs[lr * (OZ_BN + 1) + cb + j] = v;
+      }
+    }
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * OZ_EPI_WARPS) : "memory");  // the epilogue warps only
+    if (!epi_fail_sh) {
+      const int et = threadIdx.x - 64;
+      double* out = nsplit == 1 ? C + int64_t(bz) * sC : part + (int64_t(sz) * batch + bz) * M * N;
+      const int64_t ldo = nsplit == 1 ? ldc : N;
+      for (int idx = et; idx < OZ_BM * OZ_BN; idx += 32 * OZ_EPI_WARPS) {
+        const int r = idx / OZ_BN, c = idx % OZ_BN;
+        if (m0 + r < M && n0 + c < N) {
+          double v = Cs[r * (OZ_BN + 1) + c];
+          double* o = out + int64_t(m0 + r) * ldo + n0 + c;
+          if (nsplit == 1) {
             v *= alpha;
-            if (beta != 0.0) v = fma(beta, o[j], v);
-            o[j] = v;
+            if (beta != 0.0) v = fma(beta, *o, v);
           }
-        }
-      } else {
-        double* o = part + (int64_t(sz) * batch + bz) * M * N + int64_t(row) * N + n0 + cb;
-        const int* ebc = eb + n0 + cb;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          if (n0 + cb + j < N) {
-            double v = ldexp(join_df(hi[j], lo[j]), er + row_scale_exp(ebc[j]));
-            if (row_nonfinite || ebc[j] == 2047) v = __longlong_as_double(0x7ff8000000000000LL);
-            o[j] = v;
-          }
+          *o = v;
         }
       }
     }
