@@ -110,3 +110,14 @@ def test_davidson_ex_rejects_unknown_flags():
     st = L.lib.tnx_davidson1_ex(P, P, P, P, 4, 2, 4, 5, 5, 1e-8, 100, 24, 1, 2, ctypes.byref(ev), ctypes.byref(rn),
                                 ctypes.byref(it), None, 0, None)
     assert st == L.TNX_ERR_INVALID_ARG and "flags" in _err()
+
+
+def test_profiler_families():
+    # families 0..7 (7: the Ozaki GEMM's narrow products); an empty window ends with no launches
+    for fam in range(8):
+        assert L.lib.tnx_profile_begin(fam) == L.TNX_OK
+        n, ms, fl, by = ctypes.c_int(-1), ctypes.c_double(-1), ctypes.c_double(-1), ctypes.c_double(-1)
+        assert L.lib.tnx_profile_end(ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(by)) == L.TNX_OK
+        assert (n.value, ms.value, fl.value, by.value) == (0, 0.0, 0.0, 0.0)
+    assert L.lib.tnx_profile_begin(8) == L.TNX_ERR_INVALID_ARG
+    assert L.lib.tnx_profile_begin(-1) == L.TNX_ERR_INVALID_ARG
