@@ -16,7 +16,8 @@
 // GEMM kernel: one 128 x BN output tile per CTA, 6 warps:
 //   warp 0  TMA producer (cp.async.bulk.tensor, 128B swizzle, 64-wide K slabs, 4-stage ring)
 //   warp 1  TMEM allocation + single-thread tcgen05.mma issue (kind::f16, BF16 in, FP32 acc)
-//   warps 2-5 epilogue: tcgen05.ld of the FP32 accumulator, store FP32 or FP64
+//   warps 2-5 epilogue: tcgen05.ld of the FP32 accumulator, staged through shared memory in
+//             64-column chunks, stored as FP32 or FP64 row segments
 // Every mbarrier wait is bounded (~2 s of clock); on expiry the kernel raises a flag in
 // global memory, stops issuing work, waits (bounded) for its own TMA copies and frees TMEM.
 #include <cuda.h>
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], accum_bar;
   __shared__ uint32_t tmem_base_sh;
-  __shared__ int abort_sh;
+  __shared__ int abort_sh, epi_fail_sh;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -71,6 +72,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     }
     mbar_init(smem_u32(&accum_bar), 1);
     abort_sh = 0;
+    epi_fail_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -138,31 +140,49 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     }
   } else {
     // ------------------------------------------------ epilogue (warps 2..5)
+    // The accumulator goes out in 64-column chunks through shared memory (the stage ring is free
+    // once the accumulator is complete): a thread holds one row of the tile in TMEM, and storing
+    // from there would write 32 rows per warp instruction; from shared memory every warp store
+    // covers 32 consecutive columns of one row.
     const int quad = warp & 3;  // TMEM lanes 32*quad .. 32*quad+31
-    bool ok = mbar_wait(smem_u32(&accum_bar), 0);
+    const int lr = quad * 32 + lane, et = threadIdx.x - 64;
+    const bool ok = mbar_wait(smem_u32(&accum_bar), 0);
     if (!ok) {
       if (lane == 0) atomicExch(err_flag, 1);
-    } else {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const int row = m0 + quad * 32 + lane;
+      epi_fail_sh = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    constexpr int CW = 64;  // columns per chunk; the FP64 chunk [BM][CW + 1] is 66.5 KB
+    uint8_t* stg = smem_raw + (base - smem_u32(smem_raw));
+    float* sf = reinterpret_cast<float*>(stg);
+    double* sd = reinterpret_cast<double*>(stg);
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + uint32_t(c0), r);
-        if (row < M) {
-          if (out_fp64) {
-            double* o = static_cast<double*>(out) + int64_t(row) * ldc + n0 + c0;
+    for (int c0 = 0; c0 < BN; c0 += CW) {
+      if (ok) {
+        uint32_t r[2][32];
+        tmem_ld32_async(tmem + (uint32_t(quad * 32) << 16) + uint32_t(c0), r[0]);
+        tmem_ld32_async(tmem + (uint32_t(quad * 32) << 16) + uint32_t(c0 + 32), r[1]);
+        tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (n0 + c0 + j < N) o[j] = double(__uint_as_float(r[j]));
-          } else {
-            float* o = static_cast<float*>(out) + int64_t(row) * ldc + n0 + c0;
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (n0 + c0 + j < N) o[j] = __uint_as_float(r[j]);
+          for (int j = 0; j < 32; ++j) {
+            if (out_fp64) sd[lr * (CW + 1) + h * 32 + j] = double(__uint_as_float(r[h][j]));
+            else sf[lr * (CW + 1) + h * 32 + j] = __uint_as_float(r[h][j]);
+          }
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+      if (!epi_fail_sh) {
+        for (int idx = et; idx < BM * CW; idx += 128) {
+          const int rr = idx / CW, cc = idx % CW;
+          if (m0 + rr < M && n0 + c0 + cc < N) {
+            const int64_t o = int64_t(m0 + rr) * ldc + n0 + c0 + cc;
+            if (out_fp64) static_cast<double*>(out)[o] = sd[rr * (CW + 1) + cc];
+            else static_cast<float*>(out)[o] = sf[rr * (CW + 1) + cc];
           }
         }
       }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // the chunk is out before the next one is staged
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
